@@ -1,0 +1,134 @@
+// Internal declarations shared by the host and device parts of libgbmhd.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/gbmhd.h"
+
+namespace gbmhd {
+
+constexpr int NQ = 27;        // 3x3x3 Gauss points (quadrature degree 5)
+constexpr int NQF = 9;        // 3x3 Gauss points on a face
+constexpr int NU = 81, NP = 4, NJ = 36, NPHI = 8, ND = 129;
+constexpr int OU = 0, OP = 81, OJ = 85, OPHI = 121;
+
+// Reference-element tables at the quadrature points (FP64 master copy; the
+// kernels stage an FP32 or FP64 copy in shared memory).
+struct RefTables {
+  double w[NQ];                 // Gauss weights on [0,1]^3
+  double gq1[NQ][8][3];         // Q1 geometry gradients
+  double n2[NQ][27];            // Q2 values
+  double g2[NQ][27][3];         // Q2 reference gradients
+  double p1[NQ][4];             // P1 values
+  double q1[NQ][8];             // Q1 values (φ)
+  double rt[NQ][36];            // value of the single nonzero component of each RT function
+  double rtdiv[NQ][36];         // reference divergence
+  // faces: local face f, face point t
+  double fw[NQF];                 // face weights on [0,1]^2
+  double fgq1[6][NQF][8][3];      // Q1 geometry gradients at face points
+  double frt[6][NQF][36];         // RT component value at face points
+  double frtg[6][NQF][36][3];     // reference gradient of that component
+};
+void build_ref_tables(RefTables& T);
+inline int rt_axis(int b) { return b / 12; }
+
+// Device-side float copy layouts are the same struct with float/double.
+template <typename T>
+struct DevTables {
+  T w[NQ];
+  T gq1[NQ][8][3];
+  T n2[NQ][27];
+  T g2[NQ][27][3];
+  T p1[NQ][4];
+  T q1[NQ][8];
+  T rt[NQ][36];
+  T rtdiv[NQ][36];
+};
+
+struct FacetTables {
+  double fw[NQF];
+  double fgq1[6][NQF][8][3];
+  double frt[6][NQF][36];
+  double frtg[6][NQF][36][3];
+};
+
+struct DevParams {
+  double alpha, beta, gamma, sigma;
+  double B[3], f[3], g[3];
+  double zeta_u, zeta_j;
+  int convection;
+  int has_fcell;
+};
+
+// CSR pattern + cell -> nnz map, built on the host.
+struct Pattern {
+  int64_t n = 0, nnz = 0;
+  std::vector<int64_t> rowptr;
+  std::vector<int32_t> col;
+  int32_t nclass = 0;
+  std::vector<int32_t> cell_class;     // [ncells]
+  std::vector<uint16_t> offtab;        // [nclass][ND*ND], offset of (a,b) inside row a's columns
+};
+// cell_row: [ncells][ND] global free row id or -1.  Returns "" or an error text.
+std::string build_pattern(int64_t ncells, int64_t ndofs, const int32_t* cell_row, Pattern& P);
+bool touched(int a, int b);
+
+}  // namespace gbmhd
+
+// Library context.
+struct gbmhd_ctx {
+  std::string err;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  int64_t ncells = 0, ndofs = 0, nnz = 0;
+  int64_t nfree[4] = {0, 0, 0, 0}, offs[4] = {0, 0, 0, 0}, ndir[4] = {0, 0, 0, 0};
+  int64_t nfull = 0;                   // ndofs + Dirichlet values
+  // host copies needed later
+  std::vector<int32_t> h_cell_row;
+  gbmhd::DevParams prm{};
+  // device buffers
+  double* d_cellX = nullptr;           // [ncells][24]
+  int32_t* d_gidx = nullptr;           // [ncells][129] index into d_xfull
+  int32_t* d_row = nullptr;            // [ncells][129] global free id or -1
+  uint64_t* d_sign = nullptr;          // [ncells] bit b set = RT dof b has sign -1 (or null)
+  double* d_xfull = nullptr;           // [nfull]
+  double* d_fcell = nullptr;           // [ncells][3] or null
+  int64_t nfacets = 0;
+  int32_t* d_fcellid = nullptr;
+  int8_t* d_flface = nullptr;
+  double* d_fprm = nullptr;            // [nfacets][4] tau, cw, jw, phi0
+  void* d_tab64 = nullptr;             // DevTables<double>
+  void* d_tab32 = nullptr;             // DevTables<float>
+  void* d_ftab = nullptr;              // FacetTables
+  int64_t* d_rowptr = nullptr;
+  int32_t* d_col = nullptr;
+  int32_t* d_class = nullptr;
+  uint16_t* d_offtab = nullptr;
+  int32_t nclass = 0;
+  double* d_val64 = nullptr;
+  float* d_val32 = nullptr;
+  int jac_precision = -1;              // precision of the last assembled Jacobian
+  double* d_r = nullptr;               // [ndofs] residual work vector
+  double* d_xtmp = nullptr;            // [ndofs]
+  struct Solver* solver = nullptr;     // linear-solver workspace (solver.cu)
+};
+
+// assemble.cu
+int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_jac, int precision);
+int gb_upload_tables(gbmhd_ctx* ctx);
+// param derivatives used by the adjoint: dR/dγ, dR/dcw, f_z moments (all on device)
+int gb_param_derivs(gbmhd_ctx* ctx, const double* d_x, double* d_dr_dgamma, double* d_dr_dcw,
+                    double* d_fz /*[ncells][27]*/);
+
+#define GB_CUDA(call)                                                           \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess) {                                                    \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+      return -2;                                                                \
+    }                                                                           \
+  } while (0)

@@ -1,0 +1,164 @@
+/*
+ * gbmhd.h — C ABI of the GB300 inductionless-MHD Newton assembly and solve.
+ *
+ * Drop-in for the hot path of GridapMHD.jl: the Newton Jacobian/residual
+ * assembly of the H1-HDiv weak form (u Q2, p dP1, j RT1, φ dQ1) and the sparse
+ * linear solve inside each Newton step.  A Julia host keeps
+ * `GridapMHD.main(params)` / `hunt(...)` and reaches this library with `ccall`
+ * through a new `:gb300` solver symbol.
+ *
+ * Interfaces replaced (paths inside GridapMHD.jl):
+ *   gbmhd_create        SparseMatrixAssembler + FEOperator set-up, src/main.jl:218-224,
+ *                       with the spaces of src/fespaces.jl:13-114 passed as cell dof ids
+ *   gbmhd_assemble      residual(op,xh) / jacobian(op,xh) timing entry, src/main.jl:156-165,
+ *                       integrands of src/weakforms.jl:255-312 and :721-733
+ *   gbmhd_newton_solve  _solver(::Val{:julia}) NewtonSolver + the linear solve,
+ *                       src/main.jl:181-186 and :275; Badia2024Solver FGMRES +
+ *                       block-triangular preconditioner, src/Solvers/badia2024.jl:2-48
+ *   gbmhd_adjoint       no counterpart in the reference (discrete adjoint of the solve)
+ *   gbmhd_get_csr       the assembled SparseMatrixCSR (pattern + values), for parity checks
+ *
+ * Conventions
+ *   - All host pointers are owned by the caller and only read during the call.
+ *   - Status: 0 ok; >0 not converged (report filled); <0 invalid input or CUDA error.
+ *     gbmhd_last_error() returns the message of the last failing call on a context.
+ *   - One context per host thread; calls on a context are serialised on its
+ *     own CUDA stream.
+ *   - Local dof layout of a cell (129 slots):
+ *       [0,81)   u, component-major c*27 + n, n = a + 3b + 9c over Lagrange nodes ξ ∈ {0,½,1}³
+ *       [81,85)  p, P1 nodal at (0,0,0),(1,0,0),(0,1,0),(0,0,1)
+ *       [85,121) j, RT1: d*12 + q + 3*(l1 + 2*l2), ψ = L2_q(ξ_d) L1_l1 L1_l2 e_d
+ *       [121,129) φ, Q1 nodal at the 8 vertices (a + 2b + 4c)
+ *     Local vertices are ordered a + 2b + 4c (x fastest), local faces axis*2 + side.
+ */
+#ifndef GBMHD_H
+#define GBMHD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBMHD_NDOF_CELL 129
+
+typedef struct gbmhd_ctx gbmhd_ctx;
+
+/* Cells of the mesh: trilinear hexahedra given by their 8 vertex coordinates
+ * (Gridap: get_cell_coordinates(get_grid(model))). */
+typedef struct {
+  int64_t ncells;
+  const double* cell_coords;   /* [ncells][8][3] */
+} gbmhd_mesh;
+
+/* Per-field dof numbering (Gridap: get_cell_dof_ids of each single-field space).
+ * Free ids are field-local and >= 0; Dirichlet slots hold -(id+1). */
+typedef struct {
+  int64_t nfree[4];            /* u, p, j, φ free dofs; global vector is [u;p;j;φ] */
+  int64_t ndir[4];             /* Dirichlet dofs per field */
+  const int32_t* cell_dofs;    /* [ncells][129] */
+  const double* dir_values[4]; /* Dirichlet values per field (NULL = zero) */
+  const int8_t* cell_sign_j;   /* [ncells][36] orientation ±1 of the RT dofs (NULL = +1) */
+} gbmhd_dofmap;
+
+/* Physical parameters (src/weakforms.jl:71-83, :137-178). */
+typedef struct {
+  double alpha, beta, gamma, sigma;
+  double B[3];
+  double f[3];                 /* body force when f_cell is NULL */
+  double g[3];                 /* Ohm's-law right-hand side */
+  double zeta_u, zeta_j;       /* augmented-Lagrangian weights */
+  int32_t convection;          /* 0 :none, 1 :picard, 2 :newton */
+  const double* f_cell;        /* [ncells][3] cellwise body force, or NULL */
+  /* boundary facets carrying the thin-wall law and/or a weak potential */
+  int64_t nfacets;
+  const int32_t* facet_cell;
+  const int8_t* facet_lface;   /* local face axis*2 + side */
+  const double* facet_tau;     /* penalty τ (NULL = 0) */
+  const double* facet_cw;      /* wall conductance ratio (NULL = 0) */
+  const double* facet_jw;      /* prescribed wall current (NULL = 0) */
+  const double* facet_phi0;    /* weak potential value (NULL = 0) */
+} gbmhd_params;
+
+/* Precision of the element matrices and of the preconditioner. */
+enum { GBMHD_FP64 = 0, GBMHD_MIXED = 1 };
+
+typedef struct {
+  int32_t precision;           /* GBMHD_FP64 or GBMHD_MIXED */
+  int32_t max_newton;          /* Newton iteration cap (reference :niter) */
+  double newton_rtol;          /* ‖r‖ ≤ max(atol, rtol‖r0‖) */
+  double newton_atol;
+  int32_t restart;             /* FGMRES restart length m (reference :niter_ls) */
+  int32_t max_linear;          /* FGMRES iteration cap per Newton step */
+  double linear_rtol;          /* relative tolerance of each linear solve */
+  int32_t verbose;
+} gbmhd_solve_opts;
+
+typedef struct {
+  int32_t newton_iters;
+  int32_t linear_iters;        /* summed over Newton steps */
+  int32_t converged;
+  double initial_residual, final_residual;
+  double time_assembly_s, time_setup_pc_s, time_linear_s, time_total_s;
+  double residual_history[64]; /* ‖r‖ after each Newton step (first = initial) */
+} gbmhd_report;
+
+/* Objective J(x) of the adjoint: a linear functional of the free vector,
+ * J = ∫_plane u_z dA (flow rate) or a pressure drop, given by its gradient. */
+typedef struct {
+  const double* dJdx;          /* [ndofs] ∂J/∂x, host array */
+  int32_t n_theta_cells;       /* >0: also return dJ/d f_z for every cell */
+} gbmhd_objective;
+
+int gbmhd_version(void);
+
+int gbmhd_create(gbmhd_ctx** out, const gbmhd_mesh* mesh, const gbmhd_dofmap* dofs,
+                 const gbmhd_params* params);
+
+/* Replace the physical parameters (same mesh and dofs). */
+int gbmhd_set_params(gbmhd_ctx* ctx, const gbmhd_params* params);
+
+/* Sizes: total free dofs and Jacobian nonzeros. */
+int gbmhd_sizes(const gbmhd_ctx* ctx, int64_t* ndofs, int64_t* nnz, int64_t* ncells);
+
+/* Residual r(x) (FP64) and, if want_jacobian, the Jacobian at x in the given
+ * precision, kept on the device.  x_free and r_out are host arrays [ndofs];
+ * r_out may be NULL. */
+int gbmhd_assemble(gbmhd_ctx* ctx, const double* x_free, double* r_out, int32_t want_jacobian,
+                   int32_t precision);
+
+/* Same with device pointers (inputs resident in HBM, no host traffic). */
+int gbmhd_assemble_device(gbmhd_ctx* ctx, const double* d_x_free, double* d_r_out,
+                          int32_t want_jacobian, int32_t precision);
+
+/* Copy the last assembled Jacobian to the host: rowptr [ndofs+1], col [nnz], val [nnz]
+ * (FP64; an FP32 Jacobian is widened).  Any pointer may be NULL. */
+int gbmhd_get_csr(gbmhd_ctx* ctx, int64_t* rowptr, int32_t* col, double* val);
+
+/* Newton solve from x_inout (host, [ndofs]) to convergence. */
+int gbmhd_newton_solve(gbmhd_ctx* ctx, double* x_inout, const gbmhd_solve_opts* opts,
+                       gbmhd_report* report);
+
+/* Same on a device-resident vector. */
+int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x_inout, const gbmhd_solve_opts* opts,
+                              gbmhd_report* report);
+
+/* Discrete adjoint at a converged state x (host [ndofs]): solves Jᵀλ = ∂J/∂x and
+ * returns dJ/dθ = −λᵀ ∂R/∂θ in dJ_dtheta: [0] d/dγ, [1] d/d(cw) (all thin-wall
+ * facets together), [2 .. 2+ncells) d/d f_z per cell (when n_theta_cells > 0).
+ * lambda_out (host [ndofs]) may be NULL. */
+int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x_free, const gbmhd_objective* obj,
+                  const gbmhd_solve_opts* opts, double* dJ_dtheta, int64_t ntheta, double* lambda_out,
+                  gbmhd_report* report);
+
+/* The CUDA stream (cudaStream_t) every call on this context is issued on; a
+ * host can record its own events on it to time the library's kernels. */
+void* gbmhd_get_stream(const gbmhd_ctx* ctx);
+
+const char* gbmhd_last_error(const gbmhd_ctx* ctx);
+void gbmhd_destroy(gbmhd_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBMHD_H */
