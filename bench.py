@@ -1,0 +1,265 @@
+"""Benchmark: mixed-precision Newton solve of the inductionless-MHD Hunt duct on one GPU.
+
+Workload (the GPU-scale duct configuration): Hunt duct [-1,1]^2 x 0.2, 64x64x4 hex
+cells, x,y stretched by tanh(3x)/tanh(3), periodic in z; Ha=500, Re=1 (CFD scaling
+α=1, β=1/Re, γ=Ha²/Re), B=(0,1,0), f=(0,0,1); thin-wall law cw=0.1 (τ=100) on the
+Hartmann walls, insulating side walls, no-slip walls; augmented-Lagrangian weights
+ζᵤ=ζⱼ=ZETA (they vanish at the discrete solution).  One step = one full Newton
+solve from x0 = 0 to ‖r‖ ≤ 1e-10‖r0‖: every residual/Jacobian assembly, the (u,j)
+multifrontal factorization and all FGMRES iterations.
+
+--impl reference times the FP64 CPU restatement of the reference path (the oracle:
+OpenMP cell assembly + SuperLU Newton, the semantics of GridapMHD's :julia solver)
+on a bounded sample of the same duct (a 12x12x4 mesh), in the same unit.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "gridapmhd.jl_gb300"), os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np
+
+ZETA = 3.0
+CFG = dict(nc=(64, 64), nz=4, Lz=0.2, beta_map=3.0, Ha=500.0, Re=1.0, cw=0.1, tau=100.0, zeta=ZETA)
+SAMPLE_NC = (12, 12)
+METRIC = "Newton-solve throughput (cells/s), Hunt 64x64x4 Ha=500, mixed precision"
+
+
+def workload(nc, nz, Lz, beta_map, Ha, Re, cw, tau, zeta, convection=2):
+    from helpers import hunt_case
+    return hunt_case(nc=nc, nz=nz, Ha=Ha, Re=Re, beta_map=beta_map, Lz=Lz, cw=cw, tau=tau, zeta_u=zeta,
+                     zeta_j=zeta, convection=convection)
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.samples, self.proc = [], None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([s.strip() for s in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                pass
+        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and "Active" in s[3 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def cpu_sample(steps=1):
+    """Oracle FP64 Newton (assembly + SuperLU) on the 12x12x4 sample of the same duct."""
+    from helpers import oracle_problem
+    from oracle import oracle as O
+    cfg = dict(CFG, nc=SAMPLE_NC, zeta=0.0)
+    mesh, dm, params = workload(**cfg)
+    prob = oracle_problem(mesh, dm, params)
+    times = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        O.newton_direct(prob, np.zeros(dm.ndofs), gauge=[dm.offsets["p"]], rtol=1e-10, maxiter=10)
+        times.append(time.perf_counter() - t)
+    return mesh.ncells, times
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    W, K = args.warmup, args.steps
+    nc, times = cpu_sample(W + K)
+    tk = times[W:]
+    sec = float(np.mean(tk))
+    val = nc / sec
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": val, "unit": "cells/s", "n_gpus": args.gpus, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * sec, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "hunt duct 12x12x4 sample (Lz=0.2, tanh 3, Ha=500, Re=1, cw=0.1)",
+                       "full_workload": "hunt duct 64x64x4", "solver": "Newton + SuperLU (direct)"},
+            "cpu_baseline": {"value": val, "unit": "cells/s", "cores": cores, "kind": "port",
+                             "sample": f"Newton solve of the {SAMPLE_NC[0]}x{SAMPLE_NC[1]}x4 mesh ({nc} cells); "
+                                       "assembly on all host threads, SuperLU single-threaded"},
+            "e2e": {"value": val, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    from gbmhd import _build, lib
+    from helpers import gpu_context
+    _build.build()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda")
+    t0 = time.perf_counter()
+    mesh, dm, params = workload(**CFG)
+    ctx = gpu_context(mesh, dm, params)
+    t_setup = time.perf_counter() - t0
+    n = ctx.ndofs
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    d_x = torch.zeros(n, dtype=torch.float64, device=dev)
+    opts = dict(precision=lib.GBMHD_MIXED, max_newton=12, newton_rtol=1e-10, restart=40, max_linear=400,
+                linear_rtol=1e-4)
+    reps = []
+    for _ in range(args.warmup):
+        d_x.zero_()
+        torch.cuda.synchronize()
+        rep, rc = ctx.newton_solve_device(d_x.data_ptr(), **opts)
+        reps.append(rep)
+    torch.cuda.synchronize()
+    L0 = lib.counters()
+    clk = Clocks()
+    clk.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            d_x.zero_()
+        rep, rc = ctx.newton_solve_device(d_x.data_ptr(), **opts)
+        if rc != 0:
+            raise RuntimeError(f"Newton did not converge: {rep}")
+        reps.append(rep)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = clk.stop()
+    L1 = lib.counters()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * mesh.ncells / (ms / 1e3)
+    last = reps[-1]
+    # e2e: host C-ABI call, host buffers (pinned), H2D of x0 and D2H of the solution inside
+    x_host = torch.zeros(n, dtype=torch.float64).pin_memory()
+    xh = x_host.numpy()
+    te = []
+    for _ in range(max(1, args.steps)):
+        xh[:] = 0.0
+        t = time.perf_counter()
+        x_out, rep_e, rc = ctx.newton_solve(xh, **opts)
+        te.append(time.perf_counter() - t)
+    e2e_value = world * mesh.ncells / float(np.mean(te))
+    # assembly throughput and the dominant-kernel roofline (FP32 Jacobian + FP64 residual)
+    d_r = torch.empty(n, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        ctx.assemble_device(d_x.data_ptr(), d_r.data_ptr(), True, lib.GBMHD_MIXED)
+    torch.cuda.synchronize()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nrep = 10
+    a0.record(stream)
+    for _ in range(nrep):
+        ctx.assemble_device(d_x.data_ptr(), d_r.data_ptr(), True, lib.GBMHD_MIXED)
+    a1.record(stream)
+    torch.cuda.synchronize()
+    asm_ms = a0.elapsed_time(a1) / nrep
+    j0, j1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    j0.record(stream)
+    for _ in range(nrep):
+        ctx.assemble_device(d_x.data_ptr(), 0, True, lib.GBMHD_MIXED)
+    j1.record(stream)
+    torch.cuda.synchronize()
+    jac_ms = j0.elapsed_time(j1) / nrep
+    # algorithmic bytes of one FP32 Jacobian assembly: 4 B per element-matrix contribution
+    # (14,913 per cell) + per-cell reads (coords 192 B, dof ids 2x516 B, state 1032 B)
+    alg_bytes = mesh.ncells * (14913 * 4 + 192 + 2 * 516 + 1032)
+    pk = peaks()
+    achieved = alg_bytes / (jac_ms / 1e3) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (Jacobian, preconditioner) / f64 (residual, Krylov, update)",
+            "data": "synthetic",
+            "config": {"workload": "hunt duct 64x64x4, Lz=0.2, tanh(3x) stretching, Ha=500, Re=1, cw=0.1, "
+                                   f"zeta={ZETA}", "ncells": mesh.ncells, "ndofs": n, "nnz": ctx.nnz,
+                       "precision": "mixed", "newton_rtol": 1e-10,
+                       "l2": "inputs larger than L2 (Jacobian values alone 0.78 GB)"},
+            "newton_solve_s": ms / 1e3, "newton_iters": last["newton_iters"], "linear_iters": last["linear_iters"],
+            "time_split_s": {k: last[k] for k in ("time_assembly_s", "time_setup_pc_s", "time_linear_s")},
+            "assembly_cells_per_s": mesh.ncells / (asm_ms / 1e3), "jacobian_cells_per_s": mesh.ncells / (jac_ms / 1e3),
+            "setup_s": t_setup,
+            "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+            "gpu_launches": int(L1["launches"] - L0["launches"]),
+            "library_gemm_calls": int(L1["gemm_calls"] - L0["gemm_calls"]),
+            "roofline": {"kernel": "k_cells<float,JAC> (FP32 Jacobian assembly)", "bound": "hbm",
+                         "achieved": achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": achieved / pk.get("hbm_gbs"), "traffic": None,
+                         "note": "of measured" if not pk.get("fallback") else "of fallback"},
+            "clocks": clocks}
+    if not args.no_cpu and rank == 0:
+        nc_s, times = cpu_sample(1)
+        line["cpu_baseline"] = {"value": nc_s / times[0], "unit": "cells/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"FP64 oracle Newton + SuperLU on the {SAMPLE_NC[0]}x{SAMPLE_NC[1]}x4 "
+                                          f"duct ({nc_s} cells)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

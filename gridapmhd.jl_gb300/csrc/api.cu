@@ -1,5 +1,6 @@
 // C-ABI entry points of libgbmhd (declared in include/gbmhd.h).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <string>
@@ -11,6 +12,18 @@
 using namespace gbmhd;
 
 static thread_local std::string g_create_err;
+static std::atomic<int64_t> g_launches{0}, g_gemms{0};
+
+namespace gbmhd {
+void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void count_gemm(int64_t n) { g_gemms.fetch_add(n, std::memory_order_relaxed); }
+}  // namespace gbmhd
+
+extern "C" int gbmhd_counters(int64_t* kernel_launches, int64_t* gemm_calls) {
+  if (kernel_launches) *kernel_launches = g_launches.load();
+  if (gemm_calls) *gemm_calls = g_gemms.load();
+  return 0;
+}
 
 extern "C" int gbmhd_version(void) { return 1; }
 
@@ -171,6 +184,7 @@ extern "C" int gbmhd_create(gbmhd_ctx** out, const gbmhd_mesh* mesh, const gbmhd
   ctx->nnz = P.nnz;
   ctx->nclass = P.nclass;
   ctx->h_cell_row = row;
+  ctx->h_cellX.assign(mesh->cell_coords, mesh->cell_coords + 24 * nc);
 #define ALLOC_COPY(dst, src, bytes)                                                 \
   do {                                                                              \
     cudaError_t e_ = cudaMalloc((void**)&(dst), (bytes));                           \
@@ -187,6 +201,8 @@ extern "C" int gbmhd_create(gbmhd_ctx** out, const gbmhd_mesh* mesh, const gbmhd
   ALLOC_COPY(ctx->d_class, P.cell_class.data(), sizeof(int32_t) * nc);
   ALLOC_COPY(ctx->d_offtab, P.offtab.data(), sizeof(uint16_t) * P.offtab.size());
 #undef ALLOC_COPY
+  ctx->h_rowptr.swap(P.rowptr);
+  ctx->h_col.swap(P.col);
   if (cudaMalloc(&ctx->d_r, sizeof(double) * std::max<int64_t>(ctx->ndofs, 1)) != cudaSuccess ||
       cudaMalloc(&ctx->d_xtmp, sizeof(double) * std::max<int64_t>(ctx->ndofs, 1)) != cudaSuccess) {
     ctx->err = "device allocation of work vectors failed";

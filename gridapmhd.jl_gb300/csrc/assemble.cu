@@ -588,7 +588,7 @@ static int launch_cells(gbmhd_ctx* ctx, KArgs& a, const void* tab) {
   if (grid < 1) grid = 1;
   const GeoTables* geo = reinterpret_cast<const GeoTables*>(
       reinterpret_cast<const char*>(ctx->d_tab64) + ((sizeof(DevTables<double>) + 255) & ~size_t(255)));
-  kern<<<(unsigned)grid, 256, sm, ctx->stream>>>(a, reinterpret_cast<const DevTables<T>*>(tab), geo);
+  { kern<<<(unsigned)grid, 256, sm, ctx->stream>>>(a, reinterpret_cast<const DevTables<T>*>(tab), geo); gbmhd::count_launch(); }
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -692,8 +692,8 @@ int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_
       }
       if ((rc = launch_cells<float, true, false>(ctx, a, ctx->d_tab32))) return rc;
       if (ctx->nfacets) {
-        if (d_r) k_facets<double, false, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft);
-        k_facets<float, true, false><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft);
+        { if (d_r) k_facets<double, false, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
+        { k_facets<float, true, false><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
       }
     } else {
       GB_CUDA(cudaMemsetAsync(ctx->d_val64, 0, sizeof(double) * ctx->nnz, ctx->stream));
@@ -701,16 +701,16 @@ int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_
       fa.val = ctx->d_val64;
       if (d_r) {
         if ((rc = launch_cells<double, true, true>(ctx, a, ctx->d_tab64))) return rc;
-        if (ctx->nfacets) k_facets<double, true, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft);
+        { if (ctx->nfacets) k_facets<double, true, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
       } else {
         if ((rc = launch_cells<double, true, false>(ctx, a, ctx->d_tab64))) return rc;
-        if (ctx->nfacets) k_facets<double, true, false><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft);
+        { if (ctx->nfacets) k_facets<double, true, false><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
       }
     }
     ctx->jac_precision = precision;
   } else if (d_r) {
     if ((rc = launch_cells<double, false, true>(ctx, a, ctx->d_tab64))) return rc;
-    if (ctx->nfacets) k_facets<double, false, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft);
+    { if (ctx->nfacets) k_facets<double, false, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
   }
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -727,9 +727,9 @@ int gb_param_derivs(gbmhd_ctx* ctx, const double* d_x, double* d_dr_dgamma, doub
   int64_t grid = ctx->num_sms * 8;
   if (grid > ctx->ncells) grid = ctx->ncells;
   if (grid < 1) grid = 1;
-  k_param_derivs<<<(unsigned)grid, 128, 0, ctx->stream>>>(
+  { k_param_derivs<<<(unsigned)grid, 128, 0, ctx->stream>>>(
       ctx->ncells, ctx->d_cellX, ctx->d_gidx, ctx->d_row, reinterpret_cast<const unsigned long long*>(ctx->d_sign),
-      ctx->d_xfull, reinterpret_cast<const DevTables<double>*>(ctx->d_tab64), geo, ctx->prm, d_dr_dgamma, d_fz);
+      ctx->d_xfull, reinterpret_cast<const DevTables<double>*>(ctx->d_tab64), geo, ctx->prm, d_dr_dgamma, d_fz); gbmhd::count_launch(); }
   GB_CUDA(cudaGetLastError());
   if (d_dr_dcw && ctx->nfacets) {
     FArgs fa{};
@@ -748,8 +748,8 @@ int gb_param_derivs(gbmhd_ctx* ctx, const double* d_x, double* d_dr_dgamma, doub
     fa.val = nullptr;
     fa.r = nullptr;
     fa.dr_dcw = d_dr_dcw;
-    k_facets<double, false, false><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(
-        fa, reinterpret_cast<const FacetTables*>(ctx->d_ftab));
+    { k_facets<double, false, false><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(
+        fa, reinterpret_cast<const FacetTables*>(ctx->d_ftab)); gbmhd::count_launch(); }
     GB_CUDA(cudaGetLastError());
   }
   return 0;

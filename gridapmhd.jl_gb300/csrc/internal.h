@@ -76,6 +76,10 @@ struct Pattern {
 std::string build_pattern(int64_t ncells, int64_t ndofs, const int32_t* cell_row, Pattern& P);
 bool touched(int a, int b);
 
+// Launch accounting (reported by gbmhd_counters).
+void count_launch(int64_t n = 1);
+void count_gemm(int64_t n = 1);
+
 }  // namespace gbmhd
 
 // Library context.
@@ -89,6 +93,9 @@ struct gbmhd_ctx {
   int64_t nfull = 0;                   // ndofs + Dirichlet values
   // host copies needed later
   std::vector<int32_t> h_cell_row;
+  std::vector<int64_t> h_rowptr;       // host copy of the CSR pattern (solver set-up)
+  std::vector<int32_t> h_col;
+  std::vector<double> h_cellX;
   gbmhd::DevParams prm{};
   // device buffers
   double* d_cellX = nullptr;           // [ncells][24]

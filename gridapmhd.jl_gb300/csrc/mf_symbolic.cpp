@@ -1,0 +1,331 @@
+// Symbolic analysis of the (u,j)-block multifrontal factorization (see mf.h).
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "mf.h"
+
+namespace gbmhd {
+
+namespace {
+
+struct TreeNode {
+  int32_t parent = -1;
+  int32_t child[2] = {-1, -1};
+  int64_t cbeg = 0, cend = 0;   // range in the permuted cell array
+  std::vector<int32_t> elim;
+  int32_t height = 0;
+};
+
+inline bool is_uj_slot(int a) { return a < OP || (a >= OJ && a < OPHI); }
+inline int field_of_slot(int a) { return a < OP ? 0 : (a < OJ ? 1 : (a < OPHI ? 2 : 3)); }
+
+}  // namespace
+
+std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t* cell_row, int64_t ndofs,
+                       const int64_t* rowptr, const int32_t* col, bool monolithic, MFSymbolic& S,
+                       int leaf_cells) {
+  S = MFSymbolic();
+  S.monolithic = monolithic;
+  auto in_slot = [&](int a) { return monolithic || is_uj_slot(a); };
+  std::vector<uint8_t> is_uj(ndofs, 0), kind(ndofs, 0);
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int a = 0; a < ND; ++a) {
+      const int32_t d = cell_row[c * ND + a];
+      if (d < 0) continue;
+      kind[d] = (uint8_t)field_of_slot(a);
+      if (in_slot(a)) is_uj[d] = 1;
+    }
+  for (int64_t d = 0; d < ndofs; ++d) S.nuj += is_uj[d];
+  // cell centres
+  std::vector<double> ctr(3 * ncells);
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int i = 0; i < 3; ++i) {
+      double s = 0.0;
+      for (int v = 0; v < 8; ++v) s += cell_coords[24 * c + 3 * v + i];
+      ctr[3 * c + i] = s / 8.0;
+    }
+  std::vector<int32_t> perm(ncells);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::vector<TreeNode> T;
+  T.reserve(4 * ncells / std::max(1, leaf_cells) + 16);
+  std::vector<int32_t> assigned(ndofs, -1);
+  std::vector<int64_t> stamp(ndofs, -1);
+  // breadth-first construction (top-down assignment of separator dofs)
+  T.emplace_back();
+  T[0].cbeg = 0;
+  T[0].cend = ncells;
+  for (size_t ni = 0; ni < T.size(); ++ni) {
+    const int64_t b = T[ni].cbeg, e = T[ni].cend, n = e - b;
+    bool split = false;
+    int64_t mid = 0;
+    if (n > leaf_cells) {
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      for (int64_t k = b; k < e; ++k)
+        for (int i = 0; i < 3; ++i) {
+          lo[i] = std::min(lo[i], ctr[3 * perm[k] + i]);
+          hi[i] = std::max(hi[i], ctr[3 * perm[k] + i]);
+        }
+      int axes[3] = {0, 1, 2};
+      std::sort(axes, axes + 3, [&](int x, int y) { return hi[x] - lo[x] > hi[y] - lo[y]; });
+      for (int ai = 0; ai < 3 && !split; ++ai) {
+        const int ax = axes[ai];
+        if (hi[ax] - lo[ax] <= 0.0) continue;
+        std::stable_sort(perm.begin() + b, perm.begin() + e,
+                         [&](int32_t x, int32_t y) { return ctr[3 * x + ax] < ctr[3 * y + ax]; });
+        // split at the coordinate change closest to the middle
+        const double tol = 1e-9 * (hi[ax] - lo[ax]);
+        int64_t best = -1, bestd = n + 1;
+        for (int64_t k = b + 1; k < e; ++k)
+          if (ctr[3 * perm[k] + ax] - ctr[3 * perm[k - 1] + ax] > tol) {
+            int64_t d = std::llabs((k - b) - n / 2);
+            if (d < bestd) { bestd = d; best = k; }
+          }
+        if (best > b && best < e) { split = true; mid = best; }
+      }
+    }
+    if (!split) {
+      // leaf: every unassigned (u,j) dof of its cells
+      for (int64_t k = b; k < e; ++k) {
+        const int64_t c = perm[k];
+        for (int a = 0; a < ND; ++a) {
+          if (!in_slot(a)) continue;
+          const int32_t d = cell_row[c * ND + a];
+          if (d >= 0 && assigned[d] < 0) {
+            assigned[d] = (int32_t)ni;
+            T[ni].elim.push_back(d);
+          }
+        }
+      }
+      continue;
+    }
+    // separator: unassigned dofs touched by both halves
+    const int64_t tagL = 2 * (int64_t)ni;
+    for (int64_t k = b; k < mid; ++k) {
+      const int64_t c = perm[k];
+      for (int a = 0; a < ND; ++a)
+        if (in_slot(a) && cell_row[c * ND + a] >= 0) stamp[cell_row[c * ND + a]] = tagL;
+    }
+    for (int64_t k = mid; k < e; ++k) {
+      const int64_t c = perm[k];
+      for (int a = 0; a < ND; ++a) {
+        if (!in_slot(a)) continue;
+        const int32_t d = cell_row[c * ND + a];
+        if (d >= 0 && stamp[d] == tagL && assigned[d] < 0) {
+          assigned[d] = (int32_t)ni;
+          T[ni].elim.push_back(d);
+        }
+      }
+    }
+    for (int s = 0; s < 2; ++s) {
+      TreeNode ch;
+      ch.parent = (int32_t)ni;
+      ch.cbeg = s == 0 ? b : mid;
+      ch.cend = s == 0 ? mid : e;
+      T[ni].child[s] = (int32_t)T.size();
+      T.push_back(ch);
+    }
+  }
+  for (int64_t d = 0; d < ndofs; ++d)
+    if (is_uj[d] && assigned[d] < 0) return "multifrontal analysis left a (u,j) dof unassigned";
+  const int64_t nn = (int64_t)T.size();
+  // pre-order intervals (children have larger ids than parents: ids are BFS order)
+  std::vector<int64_t> pre(nn), last(nn);
+  {
+    int64_t cnt = 0;
+    std::vector<std::pair<int32_t, int>> st;
+    st.push_back({0, 0});
+    while (!st.empty()) {
+      auto& [v, s] = st.back();
+      if (s == 0) pre[v] = cnt++;
+      if (s < 2 && T[v].child[s] >= 0) {
+        int32_t ch = T[v].child[s];
+        ++s;
+        st.push_back({ch, 0});
+      } else if (s < 2) {
+        ++s;
+      } else {
+        last[v] = cnt - 1;
+        st.pop_back();
+      }
+    }
+  }
+  for (int64_t v = nn - 1; v >= 0; --v)
+    for (int s = 0; s < 2; ++s)
+      if (T[v].child[s] >= 0) T[v].height = std::max(T[v].height, T[T[v].child[s]].height + 1);
+  // boundary sets
+  std::vector<std::vector<int32_t>> bnd(nn);
+  std::fill(stamp.begin(), stamp.end(), -1);
+  for (int64_t v = 0; v < nn; ++v) {
+    for (int64_t k = T[v].cbeg; k < T[v].cend; ++k) {
+      const int64_t c = perm[k];
+      for (int a = 0; a < ND; ++a) {
+        if (!in_slot(a)) continue;
+        const int32_t d = cell_row[c * ND + a];
+        if (d < 0 || stamp[d] == v) continue;
+        stamp[d] = v;
+        const int64_t p = pre[assigned[d]];
+        if (p < pre[v] || p > last[v]) bnd[v].push_back(d);
+      }
+    }
+    std::sort(bnd[v].begin(), bnd[v].end());
+    std::sort(T[v].elim.begin(), T[v].elim.end());
+  }
+  // levels by height; front ids level by level
+  int32_t nlev = T[0].height + 1;
+  std::vector<std::vector<int32_t>> bylev(nlev);
+  for (int64_t v = 0; v < nn; ++v) bylev[T[v].height].push_back((int32_t)v);
+  std::vector<int32_t> fid(nn);
+  S.levels.resize(nlev);
+  int64_t nf = 0, off = 0;
+  for (int32_t l = 0; l < nlev; ++l) {
+    MFLevel& L = S.levels[l];
+    L.first = nf;
+    L.count = (int64_t)bylev[l].size();
+    for (int32_t v : bylev[l]) {
+      L.E = std::max<int32_t>(L.E, (int32_t)T[v].elim.size());
+      L.B = std::max<int32_t>(L.B, (int32_t)bnd[v].size());
+      fid[v] = (int32_t)nf++;
+    }
+    L.E = std::max(L.E, 1);
+    L.n = L.E + L.B;
+    L.off = off;
+    off += L.count * (int64_t)L.n * L.n;
+    S.flops += (double)L.count * 2.0 * L.n * (double)L.n * L.E;
+  }
+  S.storage = off;
+  S.f_ne.resize(nf); S.f_nb.resize(nf); S.f_level.resize(nf); S.f_parent.assign(nf, -1); S.f_off.resize(nf);
+  S.elim_ptr.assign(nf + 1, 0); S.bnd_ptr.assign(nf + 1, 0);
+  for (int64_t v = 0; v < nn; ++v) {
+    const int32_t f = fid[v];
+    const int l = T[v].height;
+    S.f_ne[f] = (int32_t)T[v].elim.size();
+    S.f_nb[f] = (int32_t)bnd[v].size();
+    S.f_level[f] = l;
+    S.f_parent[f] = T[v].parent >= 0 ? fid[T[v].parent] : -1;
+    S.f_off[f] = S.levels[l].off + (int64_t)(f - S.levels[l].first) * S.levels[l].n * S.levels[l].n;
+  }
+  std::vector<int32_t> node_of(nf);
+  for (int64_t v = 0; v < nn; ++v) node_of[fid[v]] = (int32_t)v;
+  for (int64_t f = 0; f < nf; ++f) {
+    S.elim_ptr[f + 1] = S.elim_ptr[f] + S.f_ne[f];
+    S.bnd_ptr[f + 1] = S.bnd_ptr[f] + S.f_nb[f];
+  }
+  S.elim.resize(S.elim_ptr[nf]);
+  S.bnd.resize(S.bnd_ptr[nf]);
+  for (int64_t f = 0; f < nf; ++f) {
+    const TreeNode& t = T[node_of[f]];
+    std::copy(t.elim.begin(), t.elim.end(), S.elim.begin() + S.elim_ptr[f]);
+    std::copy(bnd[node_of[f]].begin(), bnd[node_of[f]].end(), S.bnd.begin() + S.bnd_ptr[f]);
+  }
+  // arrowheads, level by level
+  std::vector<std::vector<int32_t>> lsrc(nlev);
+  std::vector<std::vector<int64_t>> ldst(nlev);
+  std::string err;
+#pragma omp parallel
+  {
+    std::vector<int32_t> pos(ndofs, -1);
+    std::vector<int32_t> src;
+    std::vector<int64_t> dst;
+#pragma omp for schedule(dynamic, 1)
+    for (int32_t l = 0; l < nlev; ++l) {
+      src.clear();
+      dst.clear();
+      const MFLevel& L = S.levels[l];
+      for (int64_t f = L.first; f < L.first + L.count; ++f) {
+        const int32_t* el = S.elim.data() + S.elim_ptr[f];
+        const int32_t* bd = S.bnd.data() + S.bnd_ptr[f];
+        const int ne = S.f_ne[f], nb = S.f_nb[f];
+        for (int i = 0; i < ne; ++i) pos[el[i]] = i;
+        for (int i = 0; i < nb; ++i) pos[bd[i]] = L.E + i;
+        const int64_t base = S.f_off[f];
+        for (int i = 0; i < ne; ++i) {
+          const int32_t e = el[i];
+          for (int64_t t = rowptr[e]; t < rowptr[e + 1]; ++t) {
+            const int32_t k = col[t];
+            if (!is_uj[k] || pos[k] < 0) continue;
+            src.push_back((int32_t)t);
+            dst.push_back(base + i + (int64_t)pos[k] * L.n);
+          }
+        }
+        for (int i = 0; i < nb; ++i) {
+          const int32_t k = bd[i];
+          for (int64_t t = rowptr[k]; t < rowptr[k + 1]; ++t) {
+            const int32_t c = col[t];
+            if (!is_uj[c] || pos[c] < 0 || pos[c] >= L.E) continue;
+            src.push_back((int32_t)t);
+            dst.push_back(base + (L.E + i) + (int64_t)pos[c] * L.n);
+          }
+        }
+        for (int i = 0; i < ne; ++i) pos[el[i]] = -1;
+        for (int i = 0; i < nb; ++i) pos[bd[i]] = -1;
+      }
+      lsrc[l] = src;
+      ldst[l] = dst;
+    }
+  }
+  int64_t tot = 0;
+  for (int32_t l = 0; l < nlev; ++l) {
+    S.levels[l].ah_begin = tot;
+    tot += (int64_t)lsrc[l].size();
+    S.levels[l].ah_end = tot;
+  }
+  S.ah_src.resize(tot);
+  S.ah_dst.resize(tot);
+  for (int32_t l = 0; l < nlev; ++l) {
+    std::copy(lsrc[l].begin(), lsrc[l].end(), S.ah_src.begin() + S.levels[l].ah_begin);
+    std::copy(ldst[l].begin(), ldst[l].end(), S.ah_dst.begin() + S.levels[l].ah_begin);
+  }
+  // extend-add maps
+  S.ea_ptr.assign(nf + 1, 0);
+  for (int64_t f = 0; f < nf; ++f) S.ea_ptr[f + 1] = S.ea_ptr[f] + (S.f_parent[f] >= 0 ? S.f_nb[f] : 0);
+  S.ea_pos.resize(S.ea_ptr[nf]);
+  {
+    std::vector<int32_t> pos(ndofs, -1);
+    for (int64_t p = 0; p < nf; ++p) {
+      const MFLevel& L = S.levels[S.f_level[p]];
+      const int32_t* el = S.elim.data() + S.elim_ptr[p];
+      const int32_t* bd = S.bnd.data() + S.bnd_ptr[p];
+      for (int i = 0; i < S.f_ne[p]; ++i) pos[el[i]] = i;
+      for (int i = 0; i < S.f_nb[p]; ++i) pos[bd[i]] = L.E + i;
+      const TreeNode& t = T[node_of[p]];
+      for (int s = 0; s < 2; ++s) {
+        if (t.child[s] < 0) continue;
+        const int32_t c = fid[t.child[s]];
+        const int32_t* cb = S.bnd.data() + S.bnd_ptr[c];
+        for (int i = 0; i < S.f_nb[c]; ++i) {
+          if (pos[cb[i]] < 0) return "multifrontal analysis: child boundary not in parent front";
+          S.ea_pos[S.ea_ptr[c] + i] = pos[cb[i]];
+        }
+      }
+      for (int i = 0; i < S.f_ne[p]; ++i) pos[el[i]] = -1;
+      for (int i = 0; i < S.f_nb[p]; ++i) pos[bd[i]] = -1;
+    }
+  }
+  // children grouped by the level of their parent
+  for (int32_t l = 0; l < nlev; ++l) {
+    S.levels[l].ch_begin = (int64_t)S.child_list.size();
+    for (int64_t f = S.levels[l].first; f < S.levels[l].first + S.levels[l].count; ++f) {
+      const TreeNode& t = T[node_of[f]];
+      for (int s = 0; s < 2; ++s)
+        if (t.child[s] >= 0) S.child_list.push_back(fid[t.child[s]]);
+    }
+    S.levels[l].ch_end = (int64_t)S.child_list.size();
+  }
+  if (S.f_nb[S.levels.back().first] != 0) return "multifrontal analysis: root front has a boundary";
+  if (monolithic) {
+    for (int64_t f = 0; f < nf; ++f) {
+      const MFLevel& L = S.levels[S.f_level[f]];
+      for (int i = 0; i < S.f_ne[f]; ++i) {
+        const int32_t d = S.elim[S.elim_ptr[f] + i];
+        if (kind[d] == 1 || kind[d] == 3) {
+          S.reg_dst.push_back(S.f_off[f] + i + (int64_t)i * L.n);
+          S.reg_dof.push_back(d);
+        }
+      }
+    }
+  }
+  return err;
+}
+
+}  // namespace gbmhd

@@ -17,10 +17,12 @@ LIBPATH = os.path.join(HERE, "libgbmhd.so")
 
 GBMHD_FP64 = 0
 GBMHD_MIXED = 1
+GBMHD_PC_MONOLITHIC = 0
+GBMHD_PC_BADIA2024 = 1
 
 SYMBOLS = ["gbmhd_version", "gbmhd_create", "gbmhd_set_params", "gbmhd_sizes", "gbmhd_assemble",
            "gbmhd_assemble_device", "gbmhd_get_csr", "gbmhd_newton_solve", "gbmhd_newton_solve_device",
-           "gbmhd_adjoint", "gbmhd_get_stream", "gbmhd_last_error", "gbmhd_destroy"]
+           "gbmhd_adjoint", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -47,7 +49,7 @@ class Params(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_newton", C.c_int32), ("newton_rtol", C.c_double),
                 ("newton_atol", C.c_double), ("restart", C.c_int32), ("max_linear", C.c_int32),
-                ("linear_rtol", C.c_double), ("verbose", C.c_int32)]
+                ("linear_rtol", C.c_double), ("verbose", C.c_int32), ("preconditioner", C.c_int32)]
 
 
 class Report(C.Structure):
@@ -101,6 +103,8 @@ def load(path: Optional[str] = None):
                                 _dp, C.POINTER(Report)]
     L.gbmhd_get_stream.argtypes = [C.c_void_p]
     L.gbmhd_get_stream.restype = C.c_void_p
+    L.gbmhd_diag_uj_solve_error.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, _dp]
+    L.gbmhd_counters.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.gbmhd_destroy.argtypes = [C.c_void_p]
     L.gbmhd_destroy.restype = None
     _LIB = L
@@ -222,6 +226,12 @@ class Context:
                                               C.byref(rep)), "gbmhd_adjoint")
         return out, lam, rep.as_dict(), rc
 
+    def uj_solve_error(self, d_state: int, precision=GBMHD_MIXED) -> float:
+        e = C.c_double()
+        self._check(self.L.gbmhd_diag_uj_solve_error(self.h, C.c_void_p(d_state), int(precision), C.byref(e)),
+                    "gbmhd_diag_uj_solve_error")
+        return e.value
+
     def stream(self) -> int:
         return int(self.L.gbmhd_get_stream(self.h) or 0)
 
@@ -237,9 +247,18 @@ class Context:
             pass
 
 
+def counters() -> dict:
+    """Kernel launches and cuBLAS GEMM calls made by libgbmhd so far."""
+    L = load()
+    a, b = C.c_int64(), C.c_int64()
+    L.gbmhd_counters(C.byref(a), C.byref(b))
+    return {"launches": a.value, "gemm_calls": b.value}
+
+
 def make_opts(precision=GBMHD_MIXED, max_newton=10, newton_rtol=1e-10, newton_atol=0.0, restart=30,
-              max_linear=500, linear_rtol=1e-3, verbose=0) -> SolveOpts:
+              max_linear=500, linear_rtol=1e-3, verbose=0, preconditioner=GBMHD_PC_MONOLITHIC) -> SolveOpts:
     o = SolveOpts()
+    o.preconditioner = int(preconditioner)
     o.precision, o.max_newton = int(precision), int(max_newton)
     o.newton_rtol, o.newton_atol = float(newton_rtol), float(newton_atol)
     o.restart, o.max_linear, o.linear_rtol, o.verbose = int(restart), int(max_linear), float(linear_rtol), int(verbose)

@@ -83,6 +83,16 @@ typedef struct {
 /* Precision of the element matrices and of the preconditioner. */
 enum { GBMHD_FP64 = 0, GBMHD_MIXED = 1 };
 
+/* Preconditioner of the FGMRES linear solve.
+ *   GBMHD_PC_MONOLITHIC: nested-dissection multifrontal factorization of the whole
+ *     Jacobian, (p,p) and (φ,φ) diagonals regularised by −ε·diag(mass) (ε = 1e-3 of the
+ *     Schur-complement scale in the mixed path, 1e-10 in FP64): the direct solve of the
+ *     :julia solver as a preconditioner.
+ *   GBMHD_PC_BADIA2024: upper block-triangular [(u,j) | p | φ] with scaled mass blocks
+ *     and a multifrontal (u,j) factorization (src/Solvers/badia2024.jl:2-48); needs the
+ *     augmented-Lagrangian weights ζᵤ, ζⱼ > 0 to converge. */
+enum { GBMHD_PC_MONOLITHIC = 0, GBMHD_PC_BADIA2024 = 1 };
+
 typedef struct {
   int32_t precision;           /* GBMHD_FP64 or GBMHD_MIXED */
   int32_t max_newton;          /* Newton iteration cap (reference :niter) */
@@ -92,6 +102,7 @@ typedef struct {
   int32_t max_linear;          /* FGMRES iteration cap per Newton step */
   double linear_rtol;          /* relative tolerance of each linear solve */
   int32_t verbose;
+  int32_t preconditioner;      /* GBMHD_PC_MONOLITHIC or GBMHD_PC_BADIA2024 */
 } gbmhd_solve_opts;
 
 typedef struct {
@@ -154,6 +165,15 @@ int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x_free, const gbmhd_objective* o
 /* The CUDA stream (cudaStream_t) every call on this context is issued on; a
  * host can record its own events on it to time the library's kernels. */
 void* gbmhd_get_stream(const gbmhd_ctx* ctx);
+
+/* Diagnostic: relative error of the (u,j)-block direct solve of the preconditioner,
+ * ‖x − A_uj⁻¹(A_uj x)‖/‖x‖ for a seeded random x, with the Jacobian assembled at the
+ * device state d_state in the given precision. */
+int gbmhd_diag_uj_solve_error(gbmhd_ctx* ctx, const double* d_state, int32_t precision, double* err);
+
+/* Diagnostics: kernels launched by this library and cuBLAS GEMM calls it made
+ * since it was loaded (all contexts together). */
+int gbmhd_counters(int64_t* kernel_launches, int64_t* gemm_calls);
 
 const char* gbmhd_last_error(const gbmhd_ctx* ctx);
 void gbmhd_destroy(gbmhd_ctx* ctx);

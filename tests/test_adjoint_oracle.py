@@ -1,0 +1,48 @@
+"""The oracle's discrete adjoint against central finite differences (CPU)."""
+import numpy as np
+
+from adjoint_ref import oracle_adjoint
+from gbmhd.objectives import flow_rate
+from helpers import hunt_case, oracle_problem
+from oracle import oracle as O
+
+
+def _solve(mesh, dm, params):
+    prob = oracle_problem(mesh, dm, params)
+    x, _ = O.newton_direct(prob, np.zeros(dm.ndofs), gauge=[dm.offsets["p"]], rtol=1e-14, maxiter=10)
+    return prob, x
+
+
+def test_oracle_adjoint_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    base = dict(nc=(3, 3), nz=2, Ha=6.0, Re=5.0, beta_map=1.5, cw=0.1, Lz=0.2, zeta_u=1.0, zeta_j=1.0)
+    mesh, dm, params = hunt_case(**base)
+    fz = rng.uniform(0.9, 1.1, mesh.ncells)
+    fcell = np.stack([0 * fz, 0 * fz, fz], 1)
+    params["f_cell"] = fcell
+    g = flow_rate(mesh, dm, 0.1)
+    prob, x = _solve(mesh, dm, params)
+    dgam, dcw, dfz, _ = oracle_adjoint(prob, dm, x, g, [dm.offsets["p"]])
+
+    def J_of(p):
+        _, xx = _solve(mesh, dm, p)
+        return g @ xx
+    h = 1e-6
+    for key, ref in (("gamma", dgam),):
+        pp, pm = dict(params), dict(params)
+        pp[key] = params[key] * (1 + h); pm[key] = params[key] * (1 - h)
+        fd = (J_of(pp) - J_of(pm)) / (2 * h * params[key])
+        assert abs(fd - ref) <= 1e-6 * abs(ref), (key, fd, ref)
+    # cw (all thin-wall facets together)
+    pp, pm = dict(params), dict(params)
+    f = params["facets"]
+    cw0 = f["cw"][0]
+    pp["facets"] = dict(f, cw=f["cw"] * (1 + h)); pm["facets"] = dict(f, cw=f["cw"] * (1 - h))
+    fd = (J_of(pp) - J_of(pm)) / (2 * h * cw0)
+    assert abs(fd - dcw) <= 1e-6 * abs(dcw), (fd, dcw)
+    # two cells of the body-force field
+    for c in (0, mesh.ncells - 1):
+        fp, fm = fcell.copy(), fcell.copy()
+        fp[c, 2] *= 1 + h; fm[c, 2] *= 1 - h
+        fd = (J_of(dict(params, f_cell=fp)) - J_of(dict(params, f_cell=fm))) / (2 * h * fcell[c, 2])
+        assert abs(fd - dfz[c]) <= 1e-6 * abs(dfz).max(), (c, fd, dfz[c])

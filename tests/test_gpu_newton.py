@@ -1,0 +1,50 @@
+"""GPU Newton solve (FGMRES + Badia2024 block preconditioner with the multifrontal (u,j)
+solve) against the oracle's FP64 Newton + direct-solve solution."""
+import numpy as np
+import pytest
+
+from helpers import gpu_context, hunt_case, oracle_problem
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def field_rel_errors(dm, x, xref, p_scale=1.0):
+    """Relative L2 error of each field's dof vector.  The pressure is compared modulo a
+    constant and relative to max(‖p_ref‖, p_scale·sqrt(n_p)): the fully developed Hunt
+    pressure is constant, so its reference vector is round-off after the gauge."""
+    out = {}
+    for f in ("u", "p", "j", "phi"):
+        a = x[dm.offsets[f]:dm.offsets[f] + dm.nfree[f]].copy()
+        b = xref[dm.offsets[f]:dm.offsets[f] + dm.nfree[f]].copy()
+        den = max(np.linalg.norm(b), 1e-300)
+        if f == "p":
+            a -= a.mean()
+            b -= b.mean()
+            den = max(np.linalg.norm(b), p_scale * np.sqrt(len(b)))
+        out[f] = np.linalg.norm(a - b) / den
+    return out
+
+
+CASES = {
+    # BASELINE config 1 shape (8x8x3, Lz=0.2, Ha=10, Re=10, cw=0.01), AL weights 10
+    "cfg1": dict(nc=(8, 8), nz=3, Ha=10.0, Re=10.0, cw=0.01, Lz=0.2, zeta_u=10.0, zeta_j=10.0),
+    # stretched, high Ha, small
+    "ha200": dict(nc=(6, 6), nz=4, Ha=200.0, Re=10.0, beta_map=2.5, cw=0.1, Lz=0.2, zeta_u=3.0, zeta_j=3.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("precision", [0, 1])
+def test_newton_matches_direct_oracle(gpu_lib, name, precision):
+    mesh, dm, params = hunt_case(**CASES[name])
+    prob = oracle_problem(mesh, dm, params)
+    xref, info = O.newton_direct(prob, np.zeros(dm.ndofs), gauge=[dm.offsets["p"]], rtol=1e-13, maxiter=10)
+    ctx = gpu_context(mesh, dm, params)
+    x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), precision=precision, max_newton=12, newton_rtol=1e-10,
+                                  newton_atol=1e-10, restart=40, max_linear=400,
+                                  linear_rtol=1e-4 if precision else 1e-8)
+    assert rc == 0 and rep["converged"], rep
+    errs = field_rel_errors(dm, x, xref)
+    for f, e in errs.items():
+        assert e <= 1e-8, (f, e, rep)
