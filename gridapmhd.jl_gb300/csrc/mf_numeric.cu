@@ -450,8 +450,8 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
       int64_t g = std::min<int64_t>((nah + 255) / 256, (int64_t)ctx->num_sms * 16);
       { k_arrowhead<T, V><<<(unsigned)g, 256, 0, ctx->stream>>>(Aval, M->d.ah_src, M->d.ah_dst, L.ah_begin, L.ah_end, F); gbmhd::count_launch(); }
     }
-    if (l == 0 && d_reg && !S.reg_dst.empty()) {
-      // every p and φ dof is cell-local and therefore eliminated in a leaf (level 0)
+    if (l + 1 == S.levels.size() && d_reg && !S.reg_dst.empty()) {
+      // the global p and φ representatives are eliminated in the root front
       const int64_t nr = (int64_t)S.reg_dst.size();
       { k_reg_add<T><<<(unsigned)std::min<int64_t>((nr + 255) / 256, 4096), 256, 0, ctx->stream>>>(F, M->d.reg_dst, M->d.reg_dof, d_reg, nr); gbmhd::count_launch(); }
     }

@@ -1,6 +1,7 @@
 // Symbolic analysis of the (u,j)-block multifrontal factorization (see mf.h).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <numeric>
 
 #include "mf.h"
@@ -37,6 +38,15 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
       if (in_slot(a)) is_uj[d] = 1;
     }
   for (int64_t d = 0; d < ndofs; ++d) S.nuj += is_uj[d];
+  // Field order of elimination inside each front (u=0, p=1, j=2, φ=3 ranks).
+  int field_rank[4] = {1, 3, 0, 2};  // j, u, φ, p
+  if (const char* o = std::getenv("GBMHD_ELIM_ORDER")) {
+    // e.g. "jufp": letters in elimination order
+    for (int i = 0; o[i] && i < 4; ++i) {
+      const int f = o[i] == 'u' ? 0 : o[i] == 'p' ? 1 : o[i] == 'j' ? 2 : 3;
+      field_rank[f] = i;
+    }
+  }
   // cell centres
   std::vector<double> ctr(3 * ncells);
   for (int64_t c = 0; c < ncells; ++c)
@@ -66,8 +76,25 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
           lo[i] = std::min(lo[i], ctr[3 * perm[k] + i]);
           hi[i] = std::max(hi[i], ctr[3 * perm[k] + i]);
         }
+      // split the axis with the most cell layers (distinct centre coordinates), so that a
+      // stretched or periodic short direction is not cut before the long ones
+      int layers[3] = {0, 0, 0};
+      {
+        std::vector<double> cs(n);
+        for (int i = 0; i < 3; ++i) {
+          for (int64_t k = b; k < e; ++k) cs[k - b] = ctr[3 * perm[k] + i];
+          std::sort(cs.begin(), cs.end());
+          const double tol = 1e-9 * std::max(hi[i] - lo[i], 1e-300);
+          int cnt = n > 0 ? 1 : 0;
+          for (int64_t k = 1; k < n; ++k)
+            if (cs[k] - cs[k - 1] > tol) ++cnt;
+          layers[i] = cnt;
+        }
+      }
       int axes[3] = {0, 1, 2};
-      std::sort(axes, axes + 3, [&](int x, int y) { return hi[x] - lo[x] > hi[y] - lo[y]; });
+      std::sort(axes, axes + 3, [&](int x, int y) {
+        return layers[x] != layers[y] ? layers[x] > layers[y] : hi[x] - lo[x] > hi[y] - lo[y];
+      });
       for (int ai = 0; ai < 3 && !split; ++ai) {
         const int ax = axes[ai];
         if (hi[ax] - lo[ax] <= 0.0) continue;
@@ -129,6 +156,37 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
   for (int64_t d = 0; d < ndofs; ++d)
     if (is_uj[d] && assigned[d] < 0) return "multifrontal analysis left a (u,j) dof unassigned";
   const int64_t nn = (int64_t)T.size();
+  if (monolithic) {
+    // A subdomain whose boundary velocities and fluxes are not yet eliminated has a
+    // constant-pressure (and, with insulating walls, constant-potential) mode: its p and φ
+    // Schur pivots are singular.  Each node therefore hands one p dof and one φ dof (the
+    // representatives of those modes) up to its parent; only the root keeps the global ones.
+    std::vector<int32_t> up_p(nn, -1), up_f(nn, -1);
+    for (int64_t v = nn - 1; v >= 0; --v) {
+      TreeNode& t = T[v];
+      for (int s = 0; s < 2; ++s) {
+        const int32_t c = t.child[s];
+        if (c < 0) continue;
+        for (int32_t d : {up_p[c], up_f[c]})
+          if (d >= 0) { t.elim.push_back(d); assigned[d] = (int32_t)v; }
+      }
+      if (v == 0) break;
+      int32_t rp = -1, rf = -1;
+      for (int32_t d : t.elim) {
+        if (kind[d] == 1 && d > rp) rp = d;
+        if (kind[d] == 3 && d > rf) rf = d;
+      }
+      auto drop = [&](int32_t d) {
+        if (d < 0) return;
+        t.elim.erase(std::find(t.elim.begin(), t.elim.end(), d));
+        assigned[d] = -2;  // re-assigned by the parent
+      };
+      drop(rp);
+      drop(rf);
+      up_p[v] = rp;
+      up_f[v] = rf;
+    }
+  }
   // pre-order intervals (children have larger ids than parents: ids are BFS order)
   std::vector<int64_t> pre(nn), last(nn);
   {
@@ -169,7 +227,11 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
       }
     }
     std::sort(bnd[v].begin(), bnd[v].end());
-    std::sort(T[v].elim.begin(), T[v].elim.end());
+    // elimination order inside a front: field rank, then dof id
+    std::sort(T[v].elim.begin(), T[v].elim.end(), [&](int32_t x, int32_t y) {
+      const int rx = field_rank[kind[x]], ry = field_rank[kind[y]];
+      return rx != ry ? rx < ry : x < y;
+    });
   }
   // levels by height; front ids level by level
   int32_t nlev = T[0].height + 1;
@@ -314,7 +376,7 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
   }
   if (S.f_nb[S.levels.back().first] != 0) return "multifrontal analysis: root front has a boundary";
   if (monolithic) {
-    for (int64_t f = 0; f < nf; ++f) {
+    for (int64_t f = S.levels.back().first; f < S.levels.back().first + S.levels.back().count; ++f) {
       const MFLevel& L = S.levels[S.f_level[f]];
       for (int i = 0; i < S.f_ne[f]; ++i) {
         const int32_t d = S.elim[S.elim_ptr[f] + i];

@@ -372,8 +372,8 @@ static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
     S_CUDA(cudaMalloc(&s->seg, sizeof(int32_t) * 2 * ctx->ndofs));
     S_CUDA(cudaMemcpy(s->seg, seg.data(), sizeof(int32_t) * 2 * ctx->ndofs, cudaMemcpyHostToDevice));
   }
-  const double want_eps = precision == GBMHD_MIXED ? (std::getenv("GBMHD_PC_EPS32") ? std::atof(std::getenv("GBMHD_PC_EPS32")) : 1e-3)
-                                                   : (std::getenv("GBMHD_PC_EPS64") ? std::atof(std::getenv("GBMHD_PC_EPS64")) : 1e-10);
+  const double want_eps = precision == GBMHD_MIXED ? (std::getenv("GBMHD_PC_EPS32") ? std::atof(std::getenv("GBMHD_PC_EPS32")) : 1.0)
+                                                   : (std::getenv("GBMHD_PC_EPS64") ? std::atof(std::getenv("GBMHD_PC_EPS64")) : 1.0);
   if (!s->have_mass || s->mass_beta != ctx->prm.beta || s->mass_zu != ctx->prm.zeta_u ||
       s->mass_zj != ctx->prm.zeta_j || s->reg_eps != want_eps) {
     if (!s->Mp_inv) {
@@ -401,8 +401,9 @@ static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
     S_CUDA(cudaMemcpy(dq, q1.data(), sizeof(double) * q1.size(), cudaMemcpyHostToDevice));
     const double ap = -1.0 / (ctx->prm.beta + ctx->prm.zeta_u);
     const double af = -1.0 / (1.0 + ctx->prm.zeta_j);
-    // monolithic regularisation: ε relative to the scaled mass blocks of the Schur complements
-    double eps = precision == GBMHD_MIXED ? 1e-3 : 1e-10;
+    // monolithic: the root's global p/φ representatives get −ε·diag(mass) scaled like the
+    // Schur complements (only those pivots are singular when the walls fix u and j·n everywhere)
+    double eps = 1.0;
     if (const char* ev = std::getenv(precision == GBMHD_MIXED ? "GBMHD_PC_EPS32" : "GBMHD_PC_EPS64")) eps = std::atof(ev);
     if (!s->reg) S_CUDA(cudaMalloc(&s->reg, sizeof(double) * ctx->ndofs));
     S_CUDA(cudaMemsetAsync(s->reg, 0, sizeof(double) * ctx->ndofs, ctx->stream));

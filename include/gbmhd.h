@@ -85,9 +85,9 @@ enum { GBMHD_FP64 = 0, GBMHD_MIXED = 1 };
 
 /* Preconditioner of the FGMRES linear solve.
  *   GBMHD_PC_MONOLITHIC: nested-dissection multifrontal factorization of the whole
- *     Jacobian, (p,p) and (φ,φ) diagonals regularised by −ε·diag(mass) (ε = 1e-3 of the
- *     Schur-complement scale in the mixed path, 1e-10 in FP64): the direct solve of the
- *     :julia solver as a preconditioner.
+ *     Jacobian (the direct solve of the :julia solver, used as a preconditioner).  Each
+ *     subdomain hands one p and one φ dof (its constant modes) to its parent; the two
+ *     global ones are regularised in the root by −diag(mass) at the Schur scale.
  *   GBMHD_PC_BADIA2024: upper block-triangular [(u,j) | p | φ] with scaled mass blocks
  *     and a multifrontal (u,j) factorization (src/Solvers/badia2024.jl:2-48); needs the
  *     augmented-Lagrangian weights ζᵤ, ζⱼ > 0 to converge. */
