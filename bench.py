@@ -144,7 +144,7 @@ def run_ours(args):
     n = ctx.ndofs
     stream = torch.cuda.ExternalStream(ctx.stream())
     d_x = torch.zeros(n, dtype=torch.float64, device=dev)
-    opts = dict(precision=lib.GBMHD_MIXED, max_newton=12, newton_rtol=1e-10, restart=40, max_linear=400,
+    opts = dict(precision=lib.GBMHD_MIXED, max_newton=12, newton_rtol=1e-10, restart=100, max_linear=300,
                 linear_rtol=1e-4)
     reps = []
     for _ in range(args.warmup):
@@ -250,7 +250,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")

@@ -70,7 +70,8 @@ struct MFNumeric;
 int mf_create(gbmhd_ctx* ctx, const gbmhd::MFSymbolic& S, MFNumeric** out);
 // Factor from the Jacobian values of the given precision (GBMHD_FP64 / GBMHD_MIXED);
 // d_reg (monolithic only): value added to the diagonal of each p and φ dof.
-int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, const double* d_reg);
+// values: precision of the Jacobian values read (the FP32 factors may read FP64 values).
+int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, int values, const double* d_reg);
 // x[sys] = A⁻¹ b[sys] (or A⁻ᵀ b[sys] when transpose) on the factorized dofs;
 // b is overwritten in those entries.
 int mf_solve(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transpose);

@@ -46,6 +46,7 @@ struct MFNumeric {
   void* T2buf = nullptr;
   size_t work_bytes = 0;
   double* tsave = nullptr;     // forward-sweep values of the eliminated dofs
+  double* ybuf = nullptr;      // backward-sweep accumulators (kept zero between solves)
   int64_t* tsave_off = nullptr;  // per front
   int64_t tsave_len = 0;
   int32_t* d_err = nullptr;    // device-side status (singular pivot block)
@@ -111,6 +112,8 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
   M->tsave_len = t;
   if ((rc = upload(ctx, &M->tsave_off, toff))) return rc;
   MF_CUDA(cudaMalloc(&M->tsave, sizeof(double) * std::max<int64_t>(t, 1)));
+  MF_CUDA(cudaMalloc(&M->ybuf, sizeof(double) * std::max<int64_t>(t, 1)));
+  MF_CUDA(cudaMemset(M->ybuf, 0, sizeof(double) * std::max<int64_t>(t, 1)));
   MF_CUDA(cudaMalloc(&M->d_err, sizeof(int32_t)));
   if (cublasCreate(&M->blas) != CUBLAS_STATUS_SUCCESS) {
     ctx->err = "multifrontal: cublasCreate failed";
@@ -126,7 +129,7 @@ void mf_destroy(MFNumeric* M) {
   if (!M) return;
   void* ptrs[] = {M->d.f_ne, M->d.f_nb, M->d.f_off, M->d.elim_ptr, M->d.bnd_ptr, M->d.elim, M->d.bnd,
                   M->d.ah_src, M->d.ah_dst, M->d.child_list, M->d.ea_ptr, M->d.ea_pos, M->d.f_parent,
-                  M->d.f_level, M->d.reg_dst, M->d.reg_dof, M->F, M->Pbuf, M->Cbuf, M->Tbuf, M->T2buf, M->tsave, M->tsave_off, M->d_err};
+                  M->d.f_level, M->d.reg_dst, M->d.reg_dof, M->F, M->Pbuf, M->Cbuf, M->Tbuf, M->T2buf, M->tsave, M->ybuf, M->tsave_off, M->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (M->blas) cublasDestroy(M->blas);
@@ -377,6 +380,75 @@ __global__ void __launch_bounds__(256) k_bwd_gemv(const T* __restrict__ F, const
   }
 }
 
+// Chunked sweeps: grid (row tiles, column chunks, fronts); each thread owns one row of
+// its tile and reduces one column chunk, staged in shared memory; partial sums are
+// added atomically.  Row accesses are coalesced (column-major fronts).
+constexpr int SW_ROWS = 256;   // rows per CTA (one per thread)
+constexpr int SW_COLS = 512;   // columns per CTA
+
+// forward: b[bnd_j] += Σ_{i<E} M[E+j, i] t_i
+template <typename T>
+__global__ void __launch_bounds__(SW_ROWS) k_fwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                       double* __restrict__ b, const double* __restrict__ tsave,
+                                                       const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
+                                                       const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_nb,
+                                                       int64_t first, int n, int E) {
+  __shared__ double ts[SW_COLS];
+  const int64_t f = first + blockIdx.z;
+  const int nb = f_nb[f];
+  const int j = blockIdx.x * SW_ROWS + threadIdx.x;
+  const int c0 = blockIdx.y * SW_COLS, c1 = min(E, c0 + SW_COLS);
+  if (blockIdx.x * SW_ROWS >= nb || c0 >= E) return;
+  const double* t = tsave + toff[f];
+  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = t[c];
+  __syncthreads();
+  if (j >= nb) return;
+  const T* M = F + f_off[f] + E + j;
+  double acc = 0.0;
+#pragma unroll 4
+  for (int c = c0; c < c1; ++c) acc += (double)M[(int64_t)c * n] * ts[c - c0];
+  atomicAdd(&b[bnd[bnd_ptr[f] + j]], acc);
+}
+
+// backward: y_i = Σ_c M[i, c] v_c with v = [t ; −x_B], accumulated into ybuf (then scattered)
+template <typename T>
+__global__ void __launch_bounds__(SW_ROWS) k_bwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                       const double* __restrict__ x, const double* __restrict__ tsave,
+                                                       const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
+                                                       const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
+                                                       const int32_t* __restrict__ f_nb, double* __restrict__ ybuf,
+                                                       int64_t first, int n, int E) {
+  __shared__ double vs[SW_COLS];
+  const int64_t f = first + blockIdx.z;
+  const int ne = f_ne[f], nb = f_nb[f];
+  const int i = blockIdx.x * SW_ROWS + threadIdx.x;
+  const int c0 = blockIdx.y * SW_COLS, c1 = min(E + nb, c0 + SW_COLS);
+  if (blockIdx.x * SW_ROWS >= ne || c0 >= E + nb) return;
+  const double* t = tsave + toff[f];
+  const int32_t* bd = bnd + bnd_ptr[f];
+  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) vs[c - c0] = c < E ? t[c] : -x[bd[c - E]];
+  __syncthreads();
+  if (i >= ne) return;
+  const T* M = F + f_off[f] + i;
+  double acc = 0.0;
+#pragma unroll 4
+  for (int c = c0; c < c1; ++c) acc += (double)M[(int64_t)c * n] * vs[c - c0];
+  atomicAdd(&ybuf[toff[f] + i], acc);
+}
+
+__global__ void k_bwd_scatter(double* __restrict__ x, double* __restrict__ ybuf, const int64_t* __restrict__ toff,
+                              const int32_t* __restrict__ elim, const int64_t* __restrict__ elim_ptr,
+                              const int32_t* __restrict__ f_ne, int64_t first) {
+  const int64_t f = first + blockIdx.x;
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  double* y = ybuf + toff[f];
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+    x[el[i]] = y[i];
+    y[i] = 0.0;  // ready for the next solve
+  }
+}
+
 // ------------------------------------------------------------------ host drivers
 template <typename T>
 static cublasStatus_t gemm_sb(MFNumeric* M, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
@@ -501,12 +573,14 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
   return 0;
 }
 
-int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, const double* d_reg) {
+int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, int values, const double* d_reg) {
+  if (values == GBMHD_MIXED && !ctx->d_val32) { ctx->err = "multifrontal: no FP32 Jacobian assembled"; return -1; }
+  if (values == GBMHD_FP64 && !ctx->d_val64) { ctx->err = "multifrontal: no FP64 Jacobian assembled"; return -1; }
   if (precision == GBMHD_MIXED) {
-    if (ctx->jac_precision != GBMHD_MIXED) { ctx->err = "multifrontal: no FP32 Jacobian assembled"; return -1; }
-    return factor_impl<float, float>(ctx, M, ctx->d_val32, d_reg);
+    if (values == GBMHD_MIXED) return factor_impl<float, float>(ctx, M, ctx->d_val32, d_reg);
+    return factor_impl<float, double>(ctx, M, ctx->d_val64, d_reg);
   }
-  if (ctx->jac_precision != GBMHD_FP64) { ctx->err = "multifrontal: no FP64 Jacobian assembled"; return -1; }
+  if (values != GBMHD_FP64) { ctx->err = "multifrontal: FP64 factors need the FP64 Jacobian"; return -1; }
   return factor_impl<double, double>(ctx, M, ctx->d_val64, d_reg);
 }
 
@@ -517,29 +591,35 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
   for (size_t l = 0; l < S.levels.size(); ++l) {
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count;
-    { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne,
-                                               L.first, L.E); gbmhd::count_launch(); }
+    { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first, L.E); gbmhd::count_launch(); }
     if (L.B > 0) {
-      const size_t sm = sizeof(double) * L.E;
-      auto kf = k_fwd_gemv<T>;
-      MF_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
-      const int per = tr ? 8 : 256;
-      dim3 g((unsigned)((L.B + per - 1) / per), (unsigned)cnt);
-      { kf<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb,
-                                      L.first, L.n, L.E, tr); gbmhd::count_launch(); }
+      if (!tr) {
+        dim3 g((unsigned)((L.B + SW_ROWS - 1) / SW_ROWS), (unsigned)((L.E + SW_COLS - 1) / SW_COLS), (unsigned)cnt);
+        { k_fwd_chunk<T><<<g, SW_ROWS, 0, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, L.first, L.n, L.E); gbmhd::count_launch(); }
+      } else {
+        const size_t sm = sizeof(double) * L.E;
+        auto kf = k_fwd_gemv<T>;
+        MF_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
+        dim3 g((unsigned)((L.B + 7) / 8), (unsigned)cnt);
+        { kf<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, L.first, L.n, L.E, tr); gbmhd::count_launch(); }
+      }
     }
     MF_CUDA(cudaGetLastError());
   }
   for (int l = (int)S.levels.size() - 1; l >= 0; --l) {
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count;
-    const size_t sm = sizeof(double) * L.n;
-    auto kb = k_bwd_gemv<T>;
-    MF_CUDA(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    const int per = tr ? 8 : 256;
-    dim3 g((unsigned)((L.E + per - 1) / per), (unsigned)cnt);
-    { kb<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.bnd,
-                                    M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, tr); gbmhd::count_launch(); }
+    if (!tr) {
+      dim3 g((unsigned)((L.E + SW_ROWS - 1) / SW_ROWS), (unsigned)((L.n + SW_COLS - 1) / SW_COLS), (unsigned)cnt);
+      { k_bwd_chunk<T><<<g, SW_ROWS, 0, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, L.first, L.n, L.E); gbmhd::count_launch(); }
+      { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
+    } else {
+      const size_t sm = sizeof(double) * L.n;
+      auto kb = k_bwd_gemv<T>;
+      MF_CUDA(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      dim3 g((unsigned)((L.E + 7) / 8), (unsigned)cnt);
+      { kb<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, tr); gbmhd::count_launch(); }
+    }
     MF_CUDA(cudaGetLastError());
   }
   return 0;

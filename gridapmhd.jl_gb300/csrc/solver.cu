@@ -417,7 +417,7 @@ static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
     s->have_mass = true;
     s->mass_beta = ctx->prm.beta; s->mass_zu = ctx->prm.zeta_u; s->mass_zj = ctx->prm.zeta_j;
   }
-  int rc = mf_factor(ctx, s->mf, precision, kind == GBMHD_PC_MONOLITHIC ? s->reg : nullptr);
+  int rc = mf_factor(ctx, s->mf, precision, ctx->jac_precision, kind == GBMHD_PC_MONOLITHIC ? s->reg : nullptr);
   if (rc) return rc;
   if (t_setup) *t_setup += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return 0;
@@ -576,7 +576,10 @@ void solver_destroy(gbmhd_ctx* ctx) {
 
 static int check_opts(gbmhd_ctx* ctx, const gbmhd_solve_opts* o) {
   if (!o) { ctx->err = "solve options are NULL"; return -1; }
-  if (o->precision != GBMHD_FP64 && o->precision != GBMHD_MIXED) { ctx->err = "unknown precision"; return -1; }
+  if (o->precision != GBMHD_FP64 && o->precision != GBMHD_MIXED && o->precision != GBMHD_MIXED_F64OP) {
+    ctx->err = "unknown precision";
+    return -1;
+  }
   if (o->max_newton < 1 || o->max_newton > 60) { ctx->err = "max_newton must be in [1, 60]"; return -1; }
   if (o->restart < 1 || o->restart > 250) { ctx->err = "restart must be in [1, 250]"; return -1; }
   if (o->max_linear < 1) { ctx->err = "max_linear must be >= 1"; return -1; }
@@ -605,7 +608,9 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
   gbmhd_report R{};
   const double t_start = now_s();
   const int64_t n = ctx->ndofs;
-  const int prec = o->precision;
+  // operator (Jacobian) precision and factor precision
+  const int prec = o->precision == GBMHD_MIXED ? GBMHD_MIXED : GBMHD_FP64;
+  const int fprec = o->precision == GBMHD_FP64 ? GBMHD_FP64 : GBMHD_MIXED;
   if (prec == GBMHD_MIXED) {
     if (!ctx->d_val32) S_CUDA(cudaMalloc(&ctx->d_val32, sizeof(float) * ctx->nnz));
   } else {
@@ -637,7 +642,7 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     S_CUDA(cudaStreamSynchronize(ctx->stream));
     R.time_assembly_s += now_s() - ta;
     if (!factored) {
-      if ((rc = setup_pc(ctx, prec, o->preconditioner, &R.time_setup_pc_s))) return rc;
+      if ((rc = setup_pc(ctx, fprec, o->preconditioner, &R.time_setup_pc_s))) return rc;
       factored = true;
     }
     // solve J δ = −r  (δ in xtmp)
@@ -737,36 +742,58 @@ extern "C" int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x, const gbmhd_object
     ctx->err = "adjoint: copy failed";
     return fail(-2);
   }
-  const int prec = o->precision;
-  if (prec == GBMHD_MIXED && !ctx->d_val32) {
-    if (cudaMalloc(&ctx->d_val32, sizeof(float) * ctx->nnz)) { ctx->err = "adjoint: allocation"; return fail(-2); }
-  }
+  // Iterative refinement: the outer residual g − Aᵀλ uses the FP64 Jacobian; each correction
+  // solves Aᵀδ = r with FGMRES on the path's operator (FP32 Jacobian in the mixed paths) and
+  // the path's factors.
+  const int fprec = o->precision == GBMHD_FP64 ? GBMHD_FP64 : GBMHD_MIXED;
+  const int oprec = fprec;
   if (!ctx->d_val64) {
     if (cudaMalloc(&ctx->d_val64, sizeof(double) * ctx->nnz)) { ctx->err = "adjoint: allocation"; return fail(-2); }
   }
-  double ta = now_s();
-  // Preconditioner factors from the Jacobian at x in the requested precision;
-  // the transposed operator is the FP64 Jacobian.
-  if ((rc = gb_assemble_device(ctx, d_x, nullptr, 1, prec))) return fail(rc);
-  if ((rc = setup_pc(ctx, prec, o->preconditioner, &R.time_setup_pc_s))) return fail(rc);
-  if (prec == GBMHD_MIXED) {
-    if ((rc = gb_assemble_device(ctx, d_x, nullptr, 1, GBMHD_FP64))) return fail(rc);
+  if (oprec == GBMHD_MIXED && !ctx->d_val32) {
+    if (cudaMalloc(&ctx->d_val32, sizeof(float) * ctx->nnz)) { ctx->err = "adjoint: allocation"; return fail(-2); }
   }
+  double ta = now_s();
+  if ((rc = gb_assemble_device(ctx, d_x, nullptr, 1, GBMHD_FP64))) return fail(rc);
+  if (oprec == GBMHD_MIXED && (rc = gb_assemble_device(ctx, d_x, nullptr, 1, GBMHD_MIXED))) return fail(rc);
+  if ((rc = setup_pc(ctx, fprec, o->preconditioner, &R.time_setup_pc_s))) return fail(rc);
   if ((rc = build_transpose(ctx))) return fail(rc);
   cudaStreamSynchronize(ctx->stream);
   R.time_assembly_s += now_s() - ta;
   double tl = now_s();
-  int iters = 0;
-  double rel = 0.0;
-  // FP64 operator (Aᵀ) with the preconditioner in `prec`
-  {
-    // fgmres uses `precision` for both the operator and apply_pc's coupling SpMV; run it
-    // with the operator precision FP64 and let the factors keep their own precision.
-    if ((rc = fgmres(ctx, GBMHD_FP64, d_g, d_lam, o->restart, o->max_linear, o->linear_rtol, true, &iters, &rel,
-                     o->verbose)))
-      return fail(rc);
+  double *d_res = nullptr, *d_del = nullptr;
+  if (cudaMalloc(&d_res, sizeof(double) * n) || cudaMalloc(&d_del, sizeof(double) * n)) {
+    ctx->err = "adjoint: allocation";
+    if (d_res) cudaFree(d_res);
+    return fail(-2);
   }
-  R.linear_iters = iters;
+  S_CUDA(cudaMemsetAsync(d_lam, 0, sizeof(double) * n, ctx->stream));
+  S_CUDA(cudaMemcpyAsync(d_res, d_g, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  double gn = 0.0, rn = 0.0, rel = 1.0;
+  int total = 0;
+  if ((rc = dot(ctx, s, d_g, 1, d_g, &gn))) { cudaFree(d_res); cudaFree(d_del); return fail(rc); }
+  gn = std::sqrt(gn);
+  const double inner_rtol = oprec == GBMHD_MIXED ? std::max(o->linear_rtol, 1e-4) : o->linear_rtol;
+  for (int k = 0; k < 20 && gn > 0.0; ++k) {
+    int iters = 0;
+    double irel = 0.0;
+    if ((rc = fgmres(ctx, oprec, d_res, d_del, o->restart, o->max_linear, inner_rtol, true, &iters, &irel,
+                     o->verbose))) {
+      cudaFree(d_res); cudaFree(d_del);
+      return fail(rc);
+    }
+    total += iters;
+    { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, d_del, 1.0, d_lam); gbmhd::count_launch(); }
+    if ((rc = spmv_t(ctx, s, GBMHD_FP64, 0, n, d_lam, d_res))) { cudaFree(d_res); cudaFree(d_del); return fail(rc); }
+    { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, d_g, -1.0, d_res); gbmhd::count_launch(); }
+    if ((rc = dot(ctx, s, d_res, 1, d_res, &rn))) { cudaFree(d_res); cudaFree(d_del); return fail(rc); }
+    rel = std::sqrt(rn) / gn;
+    if (o->verbose) std::fprintf(stderr, "adjoint refinement %d: %d iterations, |g - Aᵀλ|/|g| = %.3e\n", k, iters, rel);
+    if (rel <= o->linear_rtol) break;
+  }
+  cudaFree(d_res);
+  cudaFree(d_del);
+  R.linear_iters = total;
   R.final_residual = rel;
   R.time_linear_s = now_s() - tl;
   if ((rc = gb_param_derivs(ctx, d_x, d_dg, d_dc, d_fz))) return fail(rc);
@@ -777,12 +804,20 @@ extern "C" int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x, const gbmhd_object
   dJ[1] = -tmp[1];
   if (obj->n_theta_cells > 0) {
     { k_fz_grad<<<grid_for(ctx, ctx->ncells), 256, 0, ctx->stream>>>(ctx->ncells, ctx->d_row, d_lam, d_fz, d_out); gbmhd::count_launch(); }
-    if (cudaMemcpy(dJ + 2, d_out, sizeof(double) * ctx->ncells, cudaMemcpyDeviceToHost)) {
+    // the context stream is non-blocking: copy on it and wait for it
+    if (cudaMemcpyAsync(dJ + 2, d_out, sizeof(double) * ctx->ncells, cudaMemcpyDeviceToHost, ctx->stream) ||
+        cudaStreamSynchronize(ctx->stream)) {
       ctx->err = "adjoint: copy failed";
       return fail(-2);
     }
   }
-  if (lambda_out) cudaMemcpy(lambda_out, d_lam, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  if (lambda_out) {
+    if (cudaMemcpyAsync(lambda_out, d_lam, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream) ||
+        cudaStreamSynchronize(ctx->stream)) {
+      ctx->err = "adjoint: copy failed";
+      return fail(-2);
+    }
+  }
   R.converged = rel <= o->linear_rtol;
   R.time_total_s = now_s() - t0;
   if (rep) *rep = R;

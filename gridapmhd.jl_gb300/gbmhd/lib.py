@@ -17,6 +17,7 @@ LIBPATH = os.path.join(HERE, "libgbmhd.so")
 
 GBMHD_FP64 = 0
 GBMHD_MIXED = 1
+GBMHD_MIXED_F64OP = 2
 GBMHD_PC_MONOLITHIC = 0
 GBMHD_PC_BADIA2024 = 1
 

@@ -80,8 +80,12 @@ typedef struct {
   const double* facet_phi0;    /* weak potential value (NULL = 0) */
 } gbmhd_params;
 
-/* Precision of the element matrices and of the preconditioner. */
-enum { GBMHD_FP64 = 0, GBMHD_MIXED = 1 };
+/* Precision of the element matrices and of the preconditioner.
+ *   GBMHD_FP64:        FP64 Jacobian (operator) and FP64 factors
+ *   GBMHD_MIXED:       FP32 Jacobian (operator) and FP32 factors
+ *   GBMHD_MIXED_F64OP: FP64 Jacobian (operator), FP32 factors
+ * The residual, the Krylov vectors, Gram-Schmidt and the Newton update are FP64 in all. */
+enum { GBMHD_FP64 = 0, GBMHD_MIXED = 1, GBMHD_MIXED_F64OP = 2 };
 
 /* Preconditioner of the FGMRES linear solve.
  *   GBMHD_PC_MONOLITHIC: nested-dissection multifrontal factorization of the whole
