@@ -3,10 +3,10 @@
 Workload (the GPU-scale duct configuration): Hunt duct [-1,1]^2 x 0.2, 64x64x4 hex
 cells, x,y stretched by tanh(3x)/tanh(3), periodic in z; Ha=500, Re=1 (CFD scaling
 α=1, β=1/Re, γ=Ha²/Re), B=(0,1,0), f=(0,0,1); thin-wall law cw=0.1 (τ=100) on the
-Hartmann walls, insulating side walls, no-slip walls; augmented-Lagrangian weights
-ζᵤ=ζⱼ=ZETA (they vanish at the discrete solution).  One step = one full Newton
-solve from x0 = 0 to ‖r‖ ≤ 1e-10‖r0‖: every residual/Jacobian assembly, the (u,j)
-multifrontal factorization and all FGMRES iterations.
+Hartmann walls, insulating side walls, no-slip walls; no augmented-Lagrangian terms
+(ζᵤ=ζⱼ=0: the reference's own Jacobian).  One step = one full Newton solve from x0 = 0
+to ‖r‖ ≤ 1e-10‖r0‖: every residual/Jacobian assembly, the nested-dissection
+multifrontal factorization of the Jacobian (FP32) and all FGMRES iterations (FP64).
 
 --impl reference times the FP64 CPU restatement of the reference path (the oracle:
 OpenMP cell assembly + SuperLU Newton, the semantics of GridapMHD's :julia solver)
@@ -28,9 +28,11 @@ for p in (ROOT, os.path.join(ROOT, "gridapmhd.jl_gb300"), os.path.join(ROOT, "te
 
 import numpy as np
 
-ZETA = 3.0
+ZETA = 0.0
 CFG = dict(nc=(64, 64), nz=4, Lz=0.2, beta_map=3.0, Ha=500.0, Re=1.0, cw=0.1, tau=100.0, zeta=ZETA)
 SAMPLE_NC = (12, 12)
+# smaller duct for kernel-level profiling captures (fits a few GB on the device)
+CFG_SMALL = dict(nc=(32, 32), nz=3, Lz=0.2, beta_map=2.0, Ha=100.0, Re=10.0, cw=0.1, tau=100.0, zeta=0.0)
 METRIC = "Newton-solve throughput (cells/s), Hunt 64x64x4 Ha=500, mixed precision"
 
 
@@ -138,7 +140,8 @@ def run_ours(args):
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     dev = torch.device("cuda")
     t0 = time.perf_counter()
-    mesh, dm, params = workload(**CFG)
+    cfg = CFG_SMALL if args.small else CFG
+    mesh, dm, params = workload(**cfg)
     ctx = gpu_context(mesh, dm, params)
     t_setup = time.perf_counter() - t0
     n = ctx.ndofs
@@ -185,12 +188,12 @@ def run_ours(args):
     x_host = torch.zeros(n, dtype=torch.float64).pin_memory()
     xh = x_host.numpy()
     te = []
-    for _ in range(max(1, args.steps)):
+    for _ in range(0 if args.no_e2e else max(1, args.steps)):
         xh[:] = 0.0
         t = time.perf_counter()
         x_out, rep_e, rc = ctx.newton_solve(xh, **opts)
         te.append(time.perf_counter() - t)
-    e2e_value = world * mesh.ncells / float(np.mean(te))
+    e2e_value = world * mesh.ncells / float(np.mean(te)) if te else None
     # assembly throughput and the dominant-kernel roofline (FP32 Jacobian + FP64 residual)
     d_r = torch.empty(n, dtype=torch.float64, device=dev)
     for _ in range(3):
@@ -254,6 +257,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--small", action="store_true", help="32x32x3 duct (profiling captures)")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -13,11 +13,15 @@
 // element blocks are formed in T (float for the mixed path, double for the
 // FP64 path) and added into the CSR values with fire-and-forget atomics at the
 // offsets of the cell's map class.  The residual is always FP64.
+#include <algorithm>
 #include <cstdio>
 
 #include "internal.h"
 
 namespace gbmhd {
+
+constexpr int CELL_THREADS = 128;  // threads of a cell CTA
+constexpr int CELL_MINB = 3;       // resident CTAs per SM the register budget is sized for
 
 template <typename T>
 struct CellWork {
@@ -73,7 +77,7 @@ __device__ __forceinline__ void red_add(float* p, float v) { atomicAdd(p, v); }
 __device__ __forceinline__ void red_add(double* p, double v) { atomicAdd(p, v); }
 
 template <typename T, bool JAC, bool RES>
-__global__ void __launch_bounds__(256) k_cells(KArgs A, const DevTables<T>* __restrict__ gtab,
+__global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, const DevTables<T>* __restrict__ gtab,
                                                const GeoTables* __restrict__ ggeo) {
   extern __shared__ __align__(16) unsigned char smem[];
   DevTables<T>& tb = *reinterpret_cast<DevTables<T>*>(smem);
@@ -310,37 +314,43 @@ __global__ void __launch_bounds__(256) k_cells(KArgs A, const DevTables<T>* __re
     const T beta = (T)P.beta, alpha = (T)P.alpha, gam = (T)P.gamma, sig = (T)P.sigma;
     const T zu = (T)P.zeta_u, zj = (T)P.zeta_j;
     const T B0 = (T)P.B[0], B1 = (T)P.B[1], B2 = (T)P.B[2];
-    // u-u: 27x27 scalar pairs, 9 component entries each
+    // u-u: 27x27 scalar pairs, 9 component entries each.  K and the Picard part first,
+    // then the Newton part one test component at a time (3 accumulators live).
     for (int idx = tid; idx < 27 * 27; idx += nth) {
       const int a = idx / 27, b = idx % 27;
       T K = 0, Cv = 0;
-      T M[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (int q = 0; q < NQ; ++q) {
         const T wd = (T)w.wdet[q];
         K += wd * (w.G[q][0][a] * w.G[q][0][b] + w.G[q][1][a] * w.G[q][1][b] + w.G[q][2][a] * w.G[q][2][b]);
         if (conv) Cv += tb.n2[q][a] * w.ugb[q][b];
-        if (newton) {
-          const T m = wd * tb.n2[q][a] * tb.n2[q][b];
-#pragma unroll
-          for (int e = 0; e < 9; ++e) M[e] += m * w.gu[q][e];  // e = d*3 + c : ∂_d u_c
-        }
       }
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
+      const T diag = beta * K + alpha * Cv;
+      for (int c = 0; c < 3; ++c) {
+        T M0 = 0, M1 = 0, M2 = 0;
+        if (newton) {
+          for (int q = 0; q < NQ; ++q) {
+            const T m = (T)w.wdet[q] * tb.n2[q][a] * tb.n2[q][b];
+            M0 += m * w.gu[q][0 * 3 + c];
+            M1 += m * w.gu[q][1 * 3 + c];
+            M2 += m * w.gu[q][2 * 3 + c];
+          }
+        }
+        const int ra = OU + c * 27 + a;
+        if (w.row[ra] < 0) continue;
+        const T Md[3] = {M0, M1, M2};
         for (int d = 0; d < 3; ++d) {
-          const int ra = OU + c * 27 + a, cb = OU + d * 27 + b;
-          if (w.row[ra] < 0 || w.row[cb] < 0) continue;
-          T v = (c == d) ? (beta * K + alpha * Cv) : (T)0;
-          if (newton) v += alpha * M[d * 3 + c];
+          const int cb = OU + d * 27 + b;
+          if (w.row[cb] < 0) continue;
+          T v = (c == d) ? diag : (T)0;
+          v += alpha * Md[d];
           if (al_u) {
-            T s = 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) s += w.Bd[k][c * 27 + a] * w.Tm[k][d * 27 + b];
-            v += zu * s;
+            T s2 = 0;
+            for (int k = 0; k < 4; ++k) s2 += w.Bd[k][c * 27 + a] * w.Tm[k][d * 27 + b];
+            v += zu * s2;
           }
           red_add(&val[w.rbase[ra] + ot[ra * ND + cb]], v);
         }
+      }
     }
     // u-p and p-u
     for (int idx = tid; idx < 81 * 4; idx += nth) {
@@ -397,6 +407,147 @@ __global__ void __launch_bounds__(256) k_cells(KArgs A, const DevTables<T>* __re
       red_add(&val[w.rbase[rj] + ot[rj * ND + rf]], -sig * s);
       red_add(&val[w.rbase[rf] + ot[rf * ND + rj]], -s);
     }
+  }
+}
+
+// ---------------------------------------------------------------------- residual (flux form)
+// One warp per cell.  Lane q < 27 evaluates the state at Gauss point q and the fluxes
+// multiplying each test-function quantity, pulled back to the reference cell:
+//   u rows: F̂g[e][c] = w det Σ_i (J⁻¹)_{e i} (β ∂_i u_c − p δ_ic),  Fv[c] = w det (α conv_c − γ (j×B)_c − f_c)
+//   j rows: F̂s[d]    = w Σ_i J_{i d} (j − σ u×B − g)_i,          F̂d   = w (−σφ + ζⱼ div j)
+//   p rows: −w det div u,   φ rows: −w det div j
+// then every lane contracts them with the reference tables for its rows (FP64 throughout).
+// Used when ζᵤ = 0 (the local pressure projection of the AL term lives in k_cells).
+constexpr int RF_WARPS = 8;
+constexpr int RF_NF = 18;
+struct ResWarp {
+  double X[24];
+  double val[ND];
+  double flux[NQ][RF_NF];
+  int32_t row[ND];
+  unsigned long long sign;
+};
+
+__global__ void __launch_bounds__(RF_WARPS * 32) k_residual_flux(KArgs A, const DevTables<double>* __restrict__ gtab,
+                                                                 const GeoTables* __restrict__ ggeo) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  DevTables<double>& tb = *reinterpret_cast<DevTables<double>*>(smem);
+  ResWarp* wsm = reinterpret_cast<ResWarp*>(smem + ((sizeof(DevTables<double>) + 15) & ~size_t(15)));
+  {
+    const double* src = reinterpret_cast<const double*>(gtab);
+    double* dst = reinterpret_cast<double*>(&tb);
+    for (int i = threadIdx.x; i < (int)(sizeof(DevTables<double>) / sizeof(double)); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  ResWarp& w = wsm[wid];
+  const DevParams& P = A.prm;
+  const int64_t nwarps = (int64_t)gridDim.x * RF_WARPS;
+  for (int64_t cell = (int64_t)blockIdx.x * RF_WARPS + wid; cell < A.ncells; cell += nwarps) {
+    if (lane < 24) w.X[lane] = A.cellX[cell * 24 + lane];
+    for (int a = lane; a < ND; a += 32) {
+      w.val[a] = A.xfull[A.gidx[cell * ND + a]];
+      w.row[a] = A.row[cell * ND + a];
+    }
+    if (lane == 0) w.sign = A.sign ? A.sign[cell] : 0ull;
+    __syncwarp();
+    if (lane < NQ) {
+      const int q = lane;
+      double J[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int a = 0; a < 3; ++a) {
+          double s = 0.0;
+          for (int v = 0; v < 8; ++v) s += w.X[3 * v + i] * ggeo->gq1[q][v][a];
+          J[i][a] = s;
+        }
+      const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      const double id = 1.0 / det;
+      double Ji[3][3];
+      Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * id;
+      Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+      Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+      Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+      Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+      Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+      Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * id;
+      Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+      Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+      const double wq = ggeo->w[q], wd = wq * det;
+      // state
+      double u[3], gu[3][3];  // gu[i][c] = ∂_i u_c
+      for (int c = 0; c < 3; ++c) {
+        double uc = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
+        for (int n = 0; n < 27; ++n) {
+          const double v = w.val[OU + c * 27 + n];
+          uc += v * tb.n2[q][n];
+          g0 += v * tb.g2[q][n][0];
+          g1 += v * tb.g2[q][n][1];
+          g2 += v * tb.g2[q][n][2];
+        }
+        u[c] = uc;
+        for (int i = 0; i < 3; ++i) gu[i][c] = Ji[0][i] * g0 + Ji[1][i] * g1 + Ji[2][i] * g2;
+      }
+      double p = 0.0;
+      for (int k = 0; k < 4; ++k) p += w.val[OP + k] * tb.p1[q][k];
+      double jr[3] = {0.0, 0.0, 0.0}, dv = 0.0;
+      for (int b = 0; b < 36; ++b) {
+        const double sv = (((w.sign >> b) & 1ull) ? -1.0 : 1.0) * w.val[OJ + b];
+        jr[b / 12] += sv * tb.rt[q][b];
+        dv += sv * tb.rtdiv[q][b];
+      }
+      double j[3];
+      for (int i = 0; i < 3; ++i) j[i] = (J[i][0] * jr[0] + J[i][1] * jr[1] + J[i][2] * jr[2]) * id;
+      const double divj = dv * id;
+      double phi = 0.0;
+      for (int k = 0; k < 8; ++k) phi += w.val[OPHI + k] * tb.q1[q][k];
+      const double* fv = P.has_fcell ? A.fcell + 3 * cell : P.f;
+      // fluxes
+      double Fg[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) Fg[i][c] = P.beta * gu[i][c] - (i == c ? p : 0.0);
+      const double jxB[3] = {j[1] * P.B[2] - j[2] * P.B[1], j[2] * P.B[0] - j[0] * P.B[2], j[0] * P.B[1] - j[1] * P.B[0]};
+      const double uxB[3] = {u[1] * P.B[2] - u[2] * P.B[1], u[2] * P.B[0] - u[0] * P.B[2], u[0] * P.B[1] - u[1] * P.B[0]};
+      double* F = w.flux[q];
+      for (int e = 0; e < 3; ++e)
+        for (int c = 0; c < 3; ++c) F[e * 3 + c] = wd * (Ji[e][0] * Fg[0][c] + Ji[e][1] * Fg[1][c] + Ji[e][2] * Fg[2][c]);
+      for (int c = 0; c < 3; ++c) {
+        double v = -P.gamma * jxB[c] - fv[c];
+        if (P.convection != 0) v += P.alpha * (gu[0][c] * u[0] + gu[1][c] * u[1] + gu[2][c] * u[2]);
+        F[9 + c] = wd * v;
+      }
+      double Fs[3];
+      for (int i = 0; i < 3; ++i) Fs[i] = j[i] - P.sigma * uxB[i] - P.g[i];
+      for (int d = 0; d < 3; ++d) F[12 + d] = wq * (Fs[0] * J[0][d] + Fs[1] * J[1][d] + Fs[2] * J[2][d]);
+      F[15] = wq * (-P.sigma * phi + P.zeta_j * divj);
+      F[16] = -wd * (gu[0][0] + gu[1][1] + gu[2][2]);
+      F[17] = -wd * divj;
+    }
+    __syncwarp();
+    for (int a = lane; a < ND; a += 32) {
+      if (w.row[a] < 0) continue;
+      double acc = 0.0;
+      if (a < OP) {
+        const int c = a / 27, n = a % 27;
+        for (int q = 0; q < NQ; ++q) {
+          const double* F = w.flux[q];
+          acc += F[c] * tb.g2[q][n][0] + F[3 + c] * tb.g2[q][n][1] + F[6 + c] * tb.g2[q][n][2] + F[9 + c] * tb.n2[q][n];
+        }
+      } else if (a < OJ) {
+        const int k = a - OP;
+        for (int q = 0; q < NQ; ++q) acc += w.flux[q][16] * tb.p1[q][k];
+      } else if (a < OPHI) {
+        const int b = a - OJ, d = b / 12;
+        for (int q = 0; q < NQ; ++q) acc += w.flux[q][12 + d] * tb.rt[q][b] + w.flux[q][15] * tb.rtdiv[q][b];
+        if ((w.sign >> b) & 1ull) acc = -acc;
+      } else {
+        const int k = a - OPHI;
+        for (int q = 0; q < NQ; ++q) acc += w.flux[q][17] * tb.q1[q][k];
+      }
+      atomicAdd(&A.r[w.row[a]], acc);
+    }
+    __syncwarp();
   }
 }
 
@@ -581,14 +732,29 @@ static int launch_cells(gbmhd_ctx* ctx, KArgs& a, const void* tab) {
   const size_t sm = cells_smem<T>();
   GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int occ = 0;
-  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, sm));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, CELL_THREADS, sm));
   if (occ < 1) { ctx->err = "assembly kernel does not fit on an SM"; return -2; }
   int64_t grid = (int64_t)ctx->num_sms * occ;
   if (grid > a.ncells) grid = a.ncells;
   if (grid < 1) grid = 1;
   const GeoTables* geo = reinterpret_cast<const GeoTables*>(
       reinterpret_cast<const char*>(ctx->d_tab64) + ((sizeof(DevTables<double>) + 255) & ~size_t(255)));
-  { kern<<<(unsigned)grid, 256, sm, ctx->stream>>>(a, reinterpret_cast<const DevTables<T>*>(tab), geo); gbmhd::count_launch(); }
+  { kern<<<(unsigned)grid, CELL_THREADS, sm, ctx->stream>>>(a, reinterpret_cast<const DevTables<T>*>(tab), geo); gbmhd::count_launch(); }
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+static int launch_residual(gbmhd_ctx* ctx, KArgs& a) {
+  if (ctx->prm.zeta_u != 0.0) return launch_cells<double, false, true>(ctx, a, ctx->d_tab64);
+  const size_t sm = ((sizeof(DevTables<double>) + 15) & ~size_t(15)) + sizeof(ResWarp) * RF_WARPS;
+  GB_CUDA(cudaFuncSetAttribute(k_residual_flux, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  int occ = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_residual_flux, RF_WARPS * 32, sm));
+  if (occ < 1) { ctx->err = "residual kernel does not fit on an SM"; return -2; }
+  int64_t grid = std::min<int64_t>((int64_t)ctx->num_sms * occ, (a.ncells + RF_WARPS - 1) / RF_WARPS);
+  const GeoTables* geo = reinterpret_cast<const GeoTables*>(
+      reinterpret_cast<const char*>(ctx->d_tab64) + ((sizeof(DevTables<double>) + 255) & ~size_t(255)));
+  { k_residual_flux<<<(unsigned)std::max<int64_t>(grid, 1), RF_WARPS * 32, sm, ctx->stream>>>(a, reinterpret_cast<const DevTables<double>*>(ctx->d_tab64), geo); gbmhd::count_launch(); }
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -688,7 +854,7 @@ int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_
       a.val = ctx->d_val32;
       fa.val = ctx->d_val32;
       if (d_r) {
-        if ((rc = launch_cells<double, false, true>(ctx, a, ctx->d_tab64))) return rc;
+        if ((rc = launch_residual(ctx, a))) return rc;
       }
       if ((rc = launch_cells<float, true, false>(ctx, a, ctx->d_tab32))) return rc;
       if (ctx->nfacets) {
@@ -700,7 +866,8 @@ int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_
       a.val = ctx->d_val64;
       fa.val = ctx->d_val64;
       if (d_r) {
-        if ((rc = launch_cells<double, true, true>(ctx, a, ctx->d_tab64))) return rc;
+        if ((rc = launch_cells<double, true, false>(ctx, a, ctx->d_tab64))) return rc;
+        if ((rc = launch_residual(ctx, a))) return rc;
         { if (ctx->nfacets) k_facets<double, true, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
       } else {
         if ((rc = launch_cells<double, true, false>(ctx, a, ctx->d_tab64))) return rc;
@@ -709,7 +876,7 @@ int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_
     }
     ctx->jac_precision = precision;
   } else if (d_r) {
-    if ((rc = launch_cells<double, false, true>(ctx, a, ctx->d_tab64))) return rc;
+    if ((rc = launch_residual(ctx, a))) return rc;
     { if (ctx->nfacets) k_facets<double, false, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
   }
   GB_CUDA(cudaGetLastError());

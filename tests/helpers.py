@@ -63,3 +63,31 @@ def gpu_context(mesh, dm, params):
 def random_state(dm, seed=1, scale=1.0):
     rng = np.random.default_rng(seed)
     return scale * rng.standard_normal(dm.ndofs)
+
+
+def expansion_case(n_up=3, n_down=6, n_y_in=3, n_y_out=3, n_z=3, Ha=20.0, Re=10.0, ratio=4.0, convection=2):
+    """Sudden expansion in MHD scaling (α=1/N, β=1/Ha², γ=1; src/Applications/expansion.jl:113-123):
+    parabolic inlet velocity, u and j Dirichlet on walls/inlet, j Dirichlet on the outlet,
+    natural (∇p-free) outlet for u, B=(0,1,0)."""
+    from gbmhd.mesh import expansion_mesh
+    mesh = expansion_mesh(n_up=n_up, n_down=n_down, n_y_in=n_y_in, n_y_out=n_y_out, n_z=n_z, ratio=ratio,
+                          L_up=1.0, L_down=2.0, grading=2.0)
+    h = mesh.meta["h_in"]
+    w = mesh.meta["width"]
+    H = mesh.meta["H"]
+
+    def u_in(P, *_):
+        # parabolic in y and z over the inlet section; mean 1 over the outlet section (flux matching)
+        y = P[:, 1] / (0.5 * h)
+        z = P[:, 2] / (0.5 * w)
+        prof = np.clip((1 - y ** 2) * (1 - z ** 2), 0.0, None)
+        scale = (H / h) * (9.0 / 4.0)  # mean of (1-y²)(1-z²) is 4/9; flux = H*w over the outlet
+        out = np.zeros((len(P), 3))
+        inlet = P[:, 0] < -mesh.meta["L_up"] + 1e-9
+        out[inlet, 0] = scale * prof[inlet]
+        return out
+    dm = build_dofmap(mesh, ["wall", "inlet"], ["wall", "inlet", "outlet"], u_values=u_in)
+    N = Ha ** 2 / Re
+    params = dict(alpha=1.0 / N, beta=1.0 / Ha ** 2, gamma=1.0, sigma=1.0, B=(0, 1, 0), f=(0.0, 0.0, 0.0),
+                  zeta_u=0.0, zeta_j=0.0, convection=convection, facets=None)
+    return mesh, dm, params

@@ -13,8 +13,7 @@ pytestmark = pytest.mark.gpu
 
 def _case():
     rng = np.random.default_rng(0)
-    mesh, dm, params = hunt_case(nc=(6, 6), nz=4, Ha=20.0, Re=10.0, beta_map=2.5, cw=0.1, Lz=0.2, zeta_u=3.0,
-                                 zeta_j=3.0)
+    mesh, dm, params = hunt_case(nc=(6, 6), nz=4, Ha=20.0, Re=10.0, beta_map=2.5, cw=0.1, Lz=0.2)
     fz = rng.uniform(0.9, 1.1, mesh.ncells)
     params["f_cell"] = np.stack([0 * fz, 0 * fz, fz], 1)
     return mesh, dm, params
