@@ -20,7 +20,8 @@
 
 namespace gbmhd {
 
-constexpr int CELL_THREADS = 128;  // threads of a cell CTA
+constexpr int CELL_THREADS = 128;  // threads of a cell CTA (single-pass phases need >= 27)
+static_assert(CELL_THREADS >= NQ && CELL_THREADS >= 24, "cell kernel phases assume one thread per Gauss point");
 constexpr int CELL_MINB = 3;       // resident CTAs per SM the register budget is sized for
 
 template <typename T>
@@ -100,11 +101,11 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
     __syncthreads();
     // ---------------------------------------------------------------- load
     if (tid < 24) w.X[tid] = A.cellX[cell * 24 + tid];
-    if (tid < ND) {
-      w.val[tid] = A.xfull[A.gidx[cell * ND + tid]];
-      int32_t rr = A.row[cell * ND + tid];
-      w.row[tid] = rr;
-      w.rbase[tid] = rr >= 0 ? A.rowptr[rr] : -1;
+    for (int a = tid; a < ND; a += nth) {  // ND = 129 slots: more than one pass for 128 threads
+      w.val[a] = A.xfull[A.gidx[cell * ND + a]];
+      const int32_t rr = A.row[cell * ND + a];
+      w.row[a] = rr;
+      w.rbase[a] = rr >= 0 ? A.rowptr[rr] : -1;
     }
     if (tid == 0) w.sign = A.sign ? A.sign[cell] : 0ull;
     __syncthreads();
