@@ -188,12 +188,13 @@ __global__ void k_extend_add(T* F, const int32_t* __restrict__ child_list, int64
 }
 
 // Inverse of the kb x kb pivot block of every front (Gauss-Jordan with partial
-// pivoting inside the block).  P[f] (NB x NB, column-major, ld NB).
+// pivoting inside the block), computed in FP64 whatever the storage type and then
+// rounded to it.  P[f] (NB x NB, column-major, ld NB).
 template <typename T>
 __global__ void __launch_bounds__(256) k_pivot_inverse(const T* __restrict__ F, int64_t off, int n, int k, int kb,
                                                        T* __restrict__ P, int32_t* err) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  T* A = reinterpret_cast<T*>(sm_raw);          // kb x 2kb, row-major [i][j]
+  double* A = reinterpret_cast<double*>(sm_raw);  // kb x 2kb, row-major [i][j]
   __shared__ int piv_row;
   __shared__ double piv_abs[256];
   __shared__ int piv_idx[256];
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(256) k_pivot_inverse(const T* __restrict__ F, 
   const int w = 2 * kb;
   for (int idx = threadIdx.x; idx < kb * w; idx += blockDim.x) {
     const int i = idx / w, j = idx % w;
-    A[idx] = j < kb ? M[(k + i) + (int64_t)(k + j) * n] : (T)((j - kb) == i ? 1 : 0);
+    A[idx] = j < kb ? (double)M[(k + i) + (int64_t)(k + j) * n] : ((j - kb) == i ? 1.0 : 0.0);
   }
   __syncthreads();
   for (int c = 0; c < kb; ++c) {
@@ -231,32 +232,32 @@ __global__ void __launch_bounds__(256) k_pivot_inverse(const T* __restrict__ F, 
     const int pr = piv_row;
     if (pr != c)
       for (int j = threadIdx.x; j < w; j += blockDim.x) {
-        T t = A[c * w + j];
+        const double t = A[c * w + j];
         A[c * w + j] = A[pr * w + j];
         A[pr * w + j] = t;
       }
     __syncthreads();
-    const T d = A[c * w + c];
-    const T inv = d != (T)0 ? (T)1 / d : (T)0;
+    const double d = A[c * w + c];
+    const double inv = d != 0.0 ? 1.0 / d : 0.0;
     __syncthreads();
     for (int j = threadIdx.x; j < w; j += blockDim.x) A[c * w + j] *= inv;
     __syncthreads();
     for (int idx = threadIdx.x; idx < kb * w; idx += blockDim.x) {
       const int i = idx / w, j = idx % w;
       if (i != c) {
-        const T m = A[i * w + c];
-        if (m != (T)0 && j != c) A[idx] -= m * A[c * w + j];
+        const double m = A[i * w + c];
+        if (m != 0.0 && j != c) A[idx] -= m * A[c * w + j];
       }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kb; i += blockDim.x)
-      if (i != c) A[i * w + c] = (T)0;
+      if (i != c) A[i * w + c] = 0.0;
     __syncthreads();
   }
   T* Pf = P + f * (int64_t)NB * NB;
   for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
     const int i = idx % NB, j = idx / NB;  // column-major
-    Pf[idx] = (i < kb && j < kb) ? A[i * w + kb + j] : (T)0;
+    Pf[idx] = (i < kb && j < kb) ? (T)A[i * w + kb + j] : (T)0;
   }
 }
 
@@ -539,9 +540,9 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
     MF_CUDA(cudaGetLastError());
     for (int k = 0; k < E; k += NB) {
       const int kb = std::min(NB, E - k);
-      const size_t sm = sizeof(T) * (size_t)kb * 2 * kb;
+      const size_t sm = sizeof(double) * (size_t)kb * 2 * kb;
       auto kinv = k_pivot_inverse<T>;
-      MF_CUDA(cudaFuncSetAttribute(kinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(T) * NB * 2 * NB)));
+      MF_CUDA(cudaFuncSetAttribute(kinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(double) * NB * 2 * NB)));
       { kinv<<<cnt, 256, sm, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
       const int64_t tot = (int64_t)n * kb;
       dim3 gc((unsigned)std::min<int64_t>((tot + 255) / 256, 1024), (unsigned)cnt);

@@ -620,9 +620,13 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
   double r0 = 0.0;
   bool factored = false;
   int status = 1;
+  // In GBMHD_MIXED the operator starts as the FP32 Jacobian (Newton with an FP32 Jacobian is
+  // iterative refinement with an FP64 residual).  When that refinement stops contracting
+  // (‖r_k‖ > 0.1‖r_{k-1}‖), the operator switches to the FP64 Jacobian; the FP32 factors stay.
+  int op_prec = prec;
   for (int it = 0;; ++it) {
     double ta = now_s();
-    if ((rc = gb_assemble_device(ctx, d_x, r, 0, prec))) return rc;
+    if ((rc = gb_assemble_device(ctx, d_x, r, 0, op_prec))) return rc;
     double rn = 0.0;
     if ((rc = dot(ctx, ctx->solver, r, 1, r, &rn))) return rc;
     rn = std::sqrt(rn);
@@ -634,11 +638,17 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     R.newton_iters = it;
     if (o->verbose) std::fprintf(stderr, "newton %d: |r| = %.6e\n", it, rn);
     if (rn <= std::max(o->newton_atol, o->newton_rtol * r0)) { status = 0; break; }
-    // attainable-accuracy stop: the FP64 residual no longer decreases and is already tiny
-    if (it >= 2 && rn > 0.9 * R.residual_history[std::min(it - 1, 63)] && rn <= 1e-6 * r0) { status = 0; break; }
+    const double prev = it > 0 ? R.residual_history[std::min(it - 1, 63)] : rn;
+    // attainable-accuracy stop (FP64 operator only): the FP64 residual no longer decreases
+    if (it >= 2 && op_prec == GBMHD_FP64 && rn > 0.9 * prev && rn <= 1e-9 * r0) { status = 0; break; }
     if (it >= o->max_newton) break;
+    if (op_prec == GBMHD_MIXED && it >= 1 && rn > 0.1 * prev) {
+      op_prec = GBMHD_FP64;
+      if (!ctx->d_val64) S_CUDA(cudaMalloc(&ctx->d_val64, sizeof(double) * ctx->nnz));
+      if (o->verbose) std::fprintf(stderr, "  operator: FP64 Jacobian from here on\n");
+    }
     ta = now_s();
-    if ((rc = gb_assemble_device(ctx, d_x, nullptr, 1, prec))) return rc;
+    if ((rc = gb_assemble_device(ctx, d_x, nullptr, 1, op_prec))) return rc;
     S_CUDA(cudaStreamSynchronize(ctx->stream));
     R.time_assembly_s += now_s() - ta;
     if (!factored) {
@@ -652,7 +662,7 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     if ((rc = ensure_workspace(ctx, o->restart))) return rc;
     { k_scale_copy<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, -1.0, r, ctx->d_xtmp); gbmhd::count_launch(); }
     // b = −r lives in d_xtmp; solution into r (reused as δ)
-    if ((rc = fgmres(ctx, prec, ctx->d_xtmp, r, o->restart, o->max_linear, o->linear_rtol, false, &iters, &rel,
+    if ((rc = fgmres(ctx, op_prec, ctx->d_xtmp, r, o->restart, o->max_linear, o->linear_rtol, false, &iters, &rel,
                      o->verbose)))
       return rc;
     R.linear_iters += iters;

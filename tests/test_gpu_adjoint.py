@@ -28,7 +28,9 @@ def test_adjoint_matches_oracle(gpu_lib, precision):
     dgam, dcw, dfz, _ = oracle_adjoint(prob, dm, xref, g, [dm.offsets["p"]])
     ctx = gpu_context(mesh, dm, params)
     x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), precision=precision, max_newton=12, newton_rtol=1e-12,
-                                  newton_atol=1e-13, restart=40, max_linear=400, linear_rtol=1e-8)
+                                  newton_atol=1e-13, restart=40, max_linear=400,
+                                  linear_rtol=1e-4 if precision else 1e-8)
+    assert rc == 0, rep
     out, lam, arep, arc = ctx.adjoint(x, g, with_cells=True, precision=precision, restart=40, max_linear=400,
                                       linear_rtol=1e-10)
     assert arc == 0, arep
@@ -46,7 +48,9 @@ def test_adjoint_matches_gpu_finite_differences(gpu_lib):
     x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), **opts)
     out, lam, arep, arc = ctx.adjoint(x, g, with_cells=False, precision=0, restart=40, max_linear=400,
                                       linear_rtol=1e-11)
-    h = 1e-6
+    # FD step 1e-5 (relative): the states come from iterative Newton solves converged to ~1e-13,
+    # whose noise enters the quotient as 1/h; the CPU test checks step 1e-6 with direct solves.
+    h = 1e-5
     gam = params["gamma"]
     Js = []
     for s in (+1, -1):
