@@ -41,8 +41,9 @@ def test_newton_matches_direct_oracle(gpu_lib, name, precision):
     prob = oracle_problem(mesh, dm, params)
     xref, info = O.newton_direct(prob, np.zeros(dm.ndofs), gauge=[dm.offsets["p"]], rtol=1e-13, maxiter=10)
     ctx = gpu_context(mesh, dm, params)
-    x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), precision=precision, max_newton=12, newton_rtol=1e-10,
-                                  newton_atol=1e-10, restart=40, max_linear=400,
+    # Stop on the relative residual alone: at Ha = 200 an absolute 1e-10 leaves p at ~1e-8.
+    x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), precision=precision, max_newton=12, newton_rtol=1e-12,
+                                  newton_atol=0.0, restart=40, max_linear=400,
                                   linear_rtol=1e-4 if precision else 1e-8)
     assert rc == 0 and rep["converged"], rep
     errs = field_rel_errors(dm, x, xref)
