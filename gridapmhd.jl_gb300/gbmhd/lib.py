@@ -23,7 +23,7 @@ GBMHD_PC_BADIA2024 = 1
 
 SYMBOLS = ["gbmhd_version", "gbmhd_create", "gbmhd_set_params", "gbmhd_sizes", "gbmhd_assemble",
            "gbmhd_assemble_device", "gbmhd_get_csr", "gbmhd_newton_solve", "gbmhd_newton_solve_device",
-           "gbmhd_adjoint", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
+           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -102,6 +102,7 @@ def load(path: Optional[str] = None):
     L.gbmhd_newton_solve_device.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(SolveOpts), C.POINTER(Report)]
     L.gbmhd_adjoint.argtypes = [C.c_void_p, _dp, C.POINTER(Objective), C.POINTER(SolveOpts), _dp, C.c_int64,
                                 _dp, C.POINTER(Report)]
+    L.gbmhd_param_gradient_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.gbmhd_get_stream.argtypes = [C.c_void_p]
     L.gbmhd_get_stream.restype = C.c_void_p
     L.gbmhd_diag_uj_solve_error.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, _dp]

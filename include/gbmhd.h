@@ -16,6 +16,8 @@
  *                       src/main.jl:181-186 and :275; Badia2024Solver FGMRES +
  *                       block-triangular preconditioner, src/Solvers/badia2024.jl:2-48
  *   gbmhd_adjoint       no counterpart in the reference (discrete adjoint of the solve)
+ *   gbmhd_param_gradient_noalloc  no counterpart in the reference (the adjoint's
+ *                       parameter gradient from a given λ, without device allocation)
  *   gbmhd_get_csr       the assembled SparseMatrixCSR (pattern + values), for parity checks
  *
  * Conventions
@@ -165,6 +167,22 @@ int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x_inout, const gbmhd_sol
 int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x_free, const gbmhd_objective* obj,
                   const gbmhd_solve_opts* opts, double* dJ_dtheta, int64_t ntheta, double* lambda_out,
                   gbmhd_report* report);
+
+/* No counterpart in the reference.  dJ/dθ = −λᵀ ∂R/∂θ for θ = (γ, cw) from a device
+ * state d_x [ndofs] and a device adjoint vector d_lambda [ndofs] (from gbmhd_adjoint's
+ * lambda_out, or the host's own solve of Jᵀλ = ∂J/∂x), written to d_out [2] on the
+ * context's stream; the call returns without waiting for it.
+ * For hosts that may not allocate device memory inside their loop (an optimiser or
+ * sampler whose device memory is held by its own pool, an embedded solver that is not
+ * allowed to call cudaMalloc/cudaFree after set-up): this call allocates nothing.  Its
+ * scratch is a file-scope device array with room for 262,144 cells and 65,536
+ * thin-wall facets (2.5 MiB per device); larger contexts are rejected with -1 and a
+ * message.  Every scratch slot that a call reads it has written first, so nothing
+ * needs zeroing.  The scratch is shared by every context on a device: calls that
+ * overlap on the GPU (several streams or host threads) race.  The first call on a
+ * device looks up the array's address with that device current; make it before any
+ * stream capture. */
+int gbmhd_param_gradient_noalloc(gbmhd_ctx* ctx, const double* d_x, const double* d_lambda, double* d_out);
 
 /* The CUDA stream (cudaStream_t) every call on this context is issued on; a
  * host can record its own events on it to time the library's kernels. */
