@@ -51,9 +51,36 @@ struct MFNumeric {
   int64_t tsave_len = 0;
   int32_t* d_err = nullptr;    // device-side status (singular pivot block)
   int fp32_gemm_mode = 0;      // 0: BF16x9 emulated FP32, 1: plain FP32
+  // sweep timing: events around each solve, harvested when the next one starts
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool ev_pending = false;
+  int64_t sweep_applies = 0;
+  double sweep_seconds = 0.0;
+  int64_t sweep_elems = 0;     // factor entries one solve reads (padding excluded)
 };
 
 int mf_precision(const MFNumeric* M) { return M ? M->precision : -1; }
+
+static void harvest_sweep_time(MFNumeric* M, bool wait) {
+  if (!M->ev_pending) return;
+  if (wait) cudaEventSynchronize(M->ev1);
+  else if (cudaEventQuery(M->ev1) != cudaSuccess) return;
+  float ms = 0.0f;
+  if (cudaEventElapsedTime(&ms, M->ev0, M->ev1) == cudaSuccess) {
+    M->sweep_seconds += 1e-3 * ms;
+    M->sweep_applies += 1;
+  }
+  M->ev_pending = false;
+}
+
+void mf_sweep_stats(MFNumeric* M, int64_t* applies, double* seconds, double* bytes_per_apply) {
+  harvest_sweep_time(M, true);
+  *applies = M->sweep_applies;
+  *seconds = M->sweep_seconds;
+  *bytes_per_apply = (double)M->sweep_elems * (M->precision == GBMHD_FP64 ? 8.0 : 4.0);
+  M->sweep_applies = 0;
+  M->sweep_seconds = 0.0;
+}
 
 #define MF_CUDA(call)                                                               \
   do {                                                                              \
@@ -110,6 +137,15 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
       t += L.E;
     }
   M->tsave_len = t;
+  // forward reads rows E.. of the ne eliminated columns, backward rows 0..ne of the ne
+  // eliminated and nb boundary columns
+  M->sweep_elems = 0;
+  for (size_t f = 0; f < S.f_ne.size(); ++f) {
+    const int64_t ne = S.f_ne[f], nb = S.f_nb[f];
+    M->sweep_elems += nb * ne + ne * (ne + nb);
+  }
+  MF_CUDA(cudaEventCreate(&M->ev0));
+  MF_CUDA(cudaEventCreate(&M->ev1));
   if ((rc = upload(ctx, &M->tsave_off, toff))) return rc;
   MF_CUDA(cudaMalloc(&M->tsave, sizeof(double) * std::max<int64_t>(t, 1)));
   MF_CUDA(cudaMalloc(&M->ybuf, sizeof(double) * std::max<int64_t>(t, 1)));
@@ -133,6 +169,8 @@ void mf_destroy(MFNumeric* M) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (M->blas) cublasDestroy(M->blas);
+  if (M->ev0) cudaEventDestroy(M->ev0);
+  if (M->ev1) cudaEventDestroy(M->ev1);
   delete M;
 }
 
@@ -308,107 +346,150 @@ __global__ void k_fwd_gather(const double* __restrict__ b, double* __restrict__ 
   for (int i = threadIdx.x; i < E; i += blockDim.x) t[i] = i < ne ? b[el[i]] : 0.0;
 }
 
-// b[bnd] += BL t  (BL = rows E.. of columns 0..E) ; transpose: b[bnd] -= TRᵀ t
+// ---- accumulation of the sweeps
+// FP32 factors: the vector entries are split into two floats (hi + lo) and the products
+// are summed in float-float arithmetic (exact product error by FMA, Knuth's TwoSum for the
+// sum), which keeps ~44 significant bits on FP32 pipes.  GB300 issues FP64 at a small
+// fraction of its FP32 rate, so an FP64 convert + FMA per factor entry would bound the
+// sweeps by FP64 issue instead of HBM; rounding the vectors to FP32 instead doubled the
+// FGMRES iteration count at Ha = 500.  FP64 factors accumulate in FP64.
 template <typename T>
-__global__ void __launch_bounds__(256) k_fwd_gemv(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                  double* __restrict__ b, const double* __restrict__ tsave,
-                                                  const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
-                                                  const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_nb,
-                                                  int64_t first, int n, int E, bool transpose) {
-  extern __shared__ double ts[];
-  const int64_t f = first + blockIdx.y;
-  const int nb = f_nb[f];
-  const double* t = tsave + toff[f];
-  for (int i = threadIdx.x; i < E; i += blockDim.x) ts[i] = t[i];
-  __syncthreads();
-  const T* M = F + f_off[f];
-  const int32_t* bd = bnd + bnd_ptr[f];
-  if (!transpose) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nb) return;
-    double acc = 0.0;
-    for (int i = 0; i < E; ++i) acc += (double)M[(E + j) + (int64_t)i * n] * ts[i];
-    atomicAdd(&b[bd[j]], acc);
-  } else {
-    // one warp per boundary dof j: column E+j, rows 0..E
-    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int j = blockIdx.x * (blockDim.x / 32) + warp;
-    if (j >= nb) return;
-    const T* colj = M + (int64_t)(E + j) * n;
-    double acc = 0.0;
-    for (int i = lane; i < E; i += 32) acc += (double)colj[i] * ts[i];
-    for (int s = 16; s > 0; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s);
-    if (lane == 0) atomicAdd(&b[bd[j]], -acc);
+struct SweepAcc;
+
+template <>
+struct SweepAcc<float> {
+  using V = float2;
+  float hi = 0.0f, lo = 0.0f;
+  __device__ static V pack(double t) {
+    const float h = (float)t;
+    return make_float2(h, (float)(t - (double)h));
   }
+  __device__ void add(float m, V v) {
+    const float p = __fmul_rn(m, v.x);
+    const float pe = fmaf(m, v.y, fmaf(m, v.x, -p));  // p + pe = m (v.x + v.y) to ~2^-48
+    const float s = __fadd_rn(hi, p);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, pe));
+  }
+  __device__ void merge(float ohi, float olo) {
+    const float s = __fadd_rn(hi, ohi);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(ohi, bp));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, olo));
+  }
+  __device__ void warp_reduce() {
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
+      merge(oh, ol);
+    }
+  }
+  __device__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <>
+struct SweepAcc<double> {
+  using V = double;
+  double a = 0.0;
+  __device__ static V pack(double t) { return t; }
+  __device__ void add(double m, V v) { a = fma(m, v, a); }
+  __device__ void warp_reduce() {
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  }
+  __device__ double value() const { return a; }
+};
+
+// Transposed sweeps (adjoint solves), one warp per column: each dot product runs down a
+// contiguous column of the column-major front.
+// forward, transposed: b[bnd_j] −= Σ_{i<ne} TR[i, j] t_i   (TR = rows 0..E of column E+j)
+template <typename T>
+__global__ void __launch_bounds__(256) k_fwd_gemv_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                    double* __restrict__ b, const double* __restrict__ tsave,
+                                                    const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
+                                                    const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_nb,
+                                                    const int32_t* __restrict__ f_ne, int64_t first, int n, int E) {
+  using V = typename SweepAcc<T>::V;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  V* ts = reinterpret_cast<V*>(sm_raw);
+  const int64_t f = first + blockIdx.y;
+  const int nb = f_nb[f], ne = f_ne[f];
+  const double* t = tsave + toff[f];
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) ts[i] = SweepAcc<T>::pack(t[i]);
+  __syncthreads();
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int j = blockIdx.x * (blockDim.x / 32) + warp;
+  if (j >= nb) return;
+  const T* colj = F + f_off[f] + (int64_t)(E + j) * n;
+  SweepAcc<T> acc;
+  for (int i = lane; i < ne; i += 32) acc.add(colj[i], ts[i]);
+  acc.warp_reduce();
+  if (lane == 0) atomicAdd(&b[bnd[bnd_ptr[f] + j]], -acc.value());
 }
 
-// x[elim] = TL t − TR x[bnd] ; transpose: x[elim] = TLᵀ t + BLᵀ x[bnd]
+// backward, transposed: x[elim_i] = Σ_{c<ne} TL[c, i] t_c + Σ_{j<nb} BL[j, i] x_B[j]
+// (column i of the front: rows 0..E are TL, rows E.. are BL)
 template <typename T>
-__global__ void __launch_bounds__(256) k_bwd_gemv(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                  double* __restrict__ x, const double* __restrict__ tsave,
-                                                  const int64_t* __restrict__ toff, const int32_t* __restrict__ elim,
-                                                  const int64_t* __restrict__ elim_ptr, const int32_t* __restrict__ bnd,
-                                                  const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
-                                                  const int32_t* __restrict__ f_nb, int64_t first, int n, int E,
-                                                  bool transpose) {
-  extern __shared__ double vs[];  // [E] t, then [n-E] x_B
+__global__ void __launch_bounds__(256) k_bwd_gemv_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                    double* __restrict__ x, const double* __restrict__ tsave,
+                                                    const int64_t* __restrict__ toff, const int32_t* __restrict__ elim,
+                                                    const int64_t* __restrict__ elim_ptr, const int32_t* __restrict__ bnd,
+                                                    const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
+                                                    const int32_t* __restrict__ f_nb, int64_t first, int n, int E) {
+  using V = typename SweepAcc<T>::V;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  V* vs = reinterpret_cast<V*>(sm_raw);  // [E] t, then [n-E] x_B
   const int64_t f = first + blockIdx.y;
   const int ne = f_ne[f], nb = f_nb[f];
   const double* t = tsave + toff[f];
   const int32_t* bd = bnd + bnd_ptr[f];
-  for (int i = threadIdx.x; i < E; i += blockDim.x) vs[i] = t[i];
-  for (int j = threadIdx.x; j < n - E; j += blockDim.x) vs[E + j] = j < nb ? x[bd[j]] : 0.0;
+  for (int i = threadIdx.x; i < ne; i += blockDim.x) vs[i] = SweepAcc<T>::pack(t[i]);
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) vs[E + j] = SweepAcc<T>::pack(x[bd[j]]);
   __syncthreads();
-  const T* M = F + f_off[f];
-  const int32_t* el = elim + elim_ptr[f];
-  if (!transpose) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ne) return;
-    double acc = 0.0;
-    for (int c = 0; c < E; ++c) acc += (double)M[i + (int64_t)c * n] * vs[c];
-    for (int j = 0; j < nb; ++j) acc -= (double)M[i + (int64_t)(E + j) * n] * vs[E + j];
-    x[el[i]] = acc;
-  } else {
-    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int i = blockIdx.x * (blockDim.x / 32) + warp;
-    if (i >= ne) return;
-    const T* coli = M + (int64_t)i * n;  // column i: rows 0..E (TL) then E.. (BL)
-    double acc = 0.0;
-    for (int c = lane; c < E; c += 32) acc += (double)coli[c] * vs[c];
-    for (int j = lane; j < nb; j += 32) acc += (double)coli[E + j] * vs[E + j];
-    for (int s = 16; s > 0; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s);
-    if (lane == 0) x[el[i]] = acc;
-  }
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int i = blockIdx.x * (blockDim.x / 32) + warp;
+  if (i >= ne) return;
+  const T* coli = F + f_off[f] + (int64_t)i * n;
+  SweepAcc<T> acc;
+  for (int c = lane; c < ne; c += 32) acc.add(coli[c], vs[c]);
+  for (int j = lane; j < nb; j += 32) acc.add(coli[E + j], vs[E + j]);
+  acc.warp_reduce();
+  if (lane == 0) x[elim[elim_ptr[f] + i]] = acc.value();
 }
 
-// Chunked sweeps: grid (row tiles, column chunks, fronts); each thread owns one row of
-// its tile and reduces one column chunk, staged in shared memory; partial sums are
-// added atomically.  Row accesses are coalesced (column-major fronts).
-constexpr int SW_ROWS = 256;   // rows per CTA (one per thread)
-constexpr int SW_COLS = 512;   // columns per CTA
+// Chunked sweeps: grid (row tiles, column chunks, fronts); each thread owns one row of its
+// tile and reduces one chunk of `cols` columns, staged in shared memory; partial sums are
+// added atomically.  Row accesses are coalesced (column-major fronts).  The chunk width is
+// chosen per level so that levels with few fronts still fill the GPU.
+constexpr int SW_ROWS = 128;  // rows per CTA (one per thread)
 
-// forward: b[bnd_j] += Σ_{i<E} M[E+j, i] t_i
+// forward: b[bnd_j] += Σ_{i<ne} M[E+j, i] t_i
 template <typename T>
 __global__ void __launch_bounds__(SW_ROWS) k_fwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
                                                        double* __restrict__ b, const double* __restrict__ tsave,
                                                        const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
                                                        const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_nb,
-                                                       int64_t first, int n, int E) {
-  __shared__ double ts[SW_COLS];
+                                                       const int32_t* __restrict__ f_ne, int64_t first, int n, int E,
+                                                       int cols) {
+  using V = typename SweepAcc<T>::V;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  V* ts = reinterpret_cast<V*>(sm_raw);
   const int64_t f = first + blockIdx.z;
   const int nb = f_nb[f];
   const int j = blockIdx.x * SW_ROWS + threadIdx.x;
-  const int c0 = blockIdx.y * SW_COLS, c1 = min(E, c0 + SW_COLS);
-  if (blockIdx.x * SW_ROWS >= nb || c0 >= E) return;
+  const int ne = f_ne[f];  // columns [ne, E) are padding
+  const int c0 = blockIdx.y * cols, c1 = min(ne, c0 + cols);
+  if (blockIdx.x * SW_ROWS >= nb || c0 >= ne) return;
   const double* t = tsave + toff[f];
-  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = t[c];
+  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = SweepAcc<T>::pack(t[c]);
   __syncthreads();
   if (j >= nb) return;
   const T* M = F + f_off[f] + E + j;
-  double acc = 0.0;
-#pragma unroll 4
-  for (int c = c0; c < c1; ++c) acc += (double)M[(int64_t)c * n] * ts[c - c0];
-  atomicAdd(&b[bnd[bnd_ptr[f] + j]], acc);
+  SweepAcc<T> acc;
+#pragma unroll 8
+  for (int c = c0; c < c1; ++c) acc.add(M[(int64_t)c * n], ts[c - c0]);
+  atomicAdd(&b[bnd[bnd_ptr[f] + j]], acc.value());
 }
 
 // backward: y_i = Σ_c M[i, c] v_c with v = [t ; −x_B], accumulated into ybuf (then scattered)
@@ -418,23 +499,31 @@ __global__ void __launch_bounds__(SW_ROWS) k_bwd_chunk(const T* __restrict__ F, 
                                                        const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
                                                        const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
                                                        const int32_t* __restrict__ f_nb, double* __restrict__ ybuf,
-                                                       int64_t first, int n, int E) {
-  __shared__ double vs[SW_COLS];
+                                                       int64_t first, int n, int E, int cols) {
+  using V = typename SweepAcc<T>::V;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  V* vs = reinterpret_cast<V*>(sm_raw);
   const int64_t f = first + blockIdx.z;
   const int ne = f_ne[f], nb = f_nb[f];
   const int i = blockIdx.x * SW_ROWS + threadIdx.x;
-  const int c0 = blockIdx.y * SW_COLS, c1 = min(E + nb, c0 + SW_COLS);
-  if (blockIdx.x * SW_ROWS >= ne || c0 >= E + nb) return;
+  // virtual columns v in [0, ne + nb): v < ne -> column v, else column E + (v − ne)
+  const int c0 = blockIdx.y * cols, c1 = min(ne + nb, c0 + cols);
+  if (blockIdx.x * SW_ROWS >= ne || c0 >= ne + nb) return;
   const double* t = tsave + toff[f];
   const int32_t* bd = bnd + bnd_ptr[f];
-  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) vs[c - c0] = c < E ? t[c] : -x[bd[c - E]];
+  for (int v = c0 + threadIdx.x; v < c1; v += blockDim.x)
+    vs[v - c0] = SweepAcc<T>::pack(v < ne ? t[v] : -x[bd[v - ne]]);
   __syncthreads();
   if (i >= ne) return;
   const T* M = F + f_off[f] + i;
-  double acc = 0.0;
-#pragma unroll 4
-  for (int c = c0; c < c1; ++c) acc += (double)M[(int64_t)c * n] * vs[c - c0];
-  atomicAdd(&ybuf[toff[f] + i], acc);
+  SweepAcc<T> acc;
+  const int va = min(c1, ne);
+#pragma unroll 8
+  for (int v = c0; v < va; ++v) acc.add(M[(int64_t)v * n], vs[v - c0]);
+  const T* MB = M + (int64_t)(E - ne) * n;
+#pragma unroll 8
+  for (int v = max(c0, ne); v < c1; ++v) acc.add(MB[(int64_t)v * n], vs[v - c0]);
+  atomicAdd(&ybuf[toff[f] + i], acc.value());
 }
 
 __global__ void k_bwd_scatter(double* __restrict__ x, double* __restrict__ ybuf, const int64_t* __restrict__ toff,
@@ -585,8 +674,21 @@ int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, int values, const dou
   return factor_impl<double, double>(ctx, M, ctx->d_val64, d_reg);
 }
 
+// Column chunk of the chunked sweeps: wide enough that the partial-sum atomics stay a
+// small fraction of the factor reads, narrow enough that a level with few fronts still
+// launches about two waves of CTAs.
+static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t fronts) {
+  const int64_t per_chunk = std::max<int64_t>(1, (rows + SW_ROWS - 1) / SW_ROWS) * std::max<int64_t>(1, fronts);
+  const int64_t want = (int64_t)ctx->num_sms * 32;  // 2 waves of 16 resident 128-thread CTAs
+  const int64_t chunks = std::max<int64_t>(1, (want + per_chunk - 1) / per_chunk);
+  int64_t cols = (ncols + chunks - 1) / chunks;
+  cols = ((cols + 31) / 32) * 32;
+  return (int)std::max<int64_t>(64, std::min<int64_t>(cols, 1024));
+}
+
 template <typename T>
 static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool tr) {
+  using V = typename SweepAcc<T>::V;
   const MFSymbolic& S = M->S;
   const T* F = reinterpret_cast<const T*>(M->F);
   for (size_t l = 0; l < S.levels.size(); ++l) {
@@ -595,14 +697,15 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first, L.E); gbmhd::count_launch(); }
     if (L.B > 0) {
       if (!tr) {
-        dim3 g((unsigned)((L.B + SW_ROWS - 1) / SW_ROWS), (unsigned)((L.E + SW_COLS - 1) / SW_COLS), (unsigned)cnt);
-        { k_fwd_chunk<T><<<g, SW_ROWS, 0, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, L.first, L.n, L.E); gbmhd::count_launch(); }
+        const int cols = sweep_cols(ctx, L.B, L.E, cnt);
+        dim3 g((unsigned)((L.B + SW_ROWS - 1) / SW_ROWS), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
+        { k_fwd_chunk<T><<<g, SW_ROWS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
       } else {
-        const size_t sm = sizeof(double) * L.E;
-        auto kf = k_fwd_gemv<T>;
+        const size_t sm = sizeof(V) * L.E;
+        auto kf = k_fwd_gemv_t<T>;
         MF_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
         dim3 g((unsigned)((L.B + 7) / 8), (unsigned)cnt);
-        { kf<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, L.first, L.n, L.E, tr); gbmhd::count_launch(); }
+        { kf<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E); gbmhd::count_launch(); }
       }
     }
     MF_CUDA(cudaGetLastError());
@@ -611,15 +714,16 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count;
     if (!tr) {
-      dim3 g((unsigned)((L.E + SW_ROWS - 1) / SW_ROWS), (unsigned)((L.n + SW_COLS - 1) / SW_COLS), (unsigned)cnt);
-      { k_bwd_chunk<T><<<g, SW_ROWS, 0, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, L.first, L.n, L.E); gbmhd::count_launch(); }
+      const int cols = sweep_cols(ctx, L.E, L.n, cnt);
+      dim3 g((unsigned)((L.E + SW_ROWS - 1) / SW_ROWS), (unsigned)((L.n + cols - 1) / cols), (unsigned)cnt);
+      { k_bwd_chunk<T><<<g, SW_ROWS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
       { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
     } else {
-      const size_t sm = sizeof(double) * L.n;
-      auto kb = k_bwd_gemv<T>;
+      const size_t sm = sizeof(V) * L.n;
+      auto kb = k_bwd_gemv_t<T>;
       MF_CUDA(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       dim3 g((unsigned)((L.E + 7) / 8), (unsigned)cnt);
-      { kb<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, tr); gbmhd::count_launch(); }
+      { kb<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E); gbmhd::count_launch(); }
     }
     MF_CUDA(cudaGetLastError());
   }
@@ -627,8 +731,19 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
 }
 
 int mf_solve(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transpose) {
-  if (M->precision == GBMHD_MIXED) return solve_impl<float>(ctx, M, d_b, d_x, transpose);
-  if (M->precision == GBMHD_FP64) return solve_impl<double>(ctx, M, d_b, d_x, transpose);
-  ctx->err = "multifrontal: not factored";
-  return -1;
+  if (M->precision != GBMHD_MIXED && M->precision != GBMHD_FP64) {
+    ctx->err = "multifrontal: not factored";
+    return -1;
+  }
+  harvest_sweep_time(M, false);
+  const bool timed = !M->ev_pending && M->ev0 && M->ev1;
+  if (timed) MF_CUDA(cudaEventRecord(M->ev0, ctx->stream));
+  const int rc = M->precision == GBMHD_MIXED ? solve_impl<float>(ctx, M, d_b, d_x, transpose)
+                                             : solve_impl<double>(ctx, M, d_b, d_x, transpose);
+  if (rc) return rc;
+  if (timed) {
+    MF_CUDA(cudaEventRecord(M->ev1, ctx->stream));
+    M->ev_pending = true;
+  }
+  return 0;
 }

@@ -39,8 +39,10 @@ struct Solver {
   double* w = nullptr;
   double* t1 = nullptr;
   double* t2 = nullptr;
+  float* x32 = nullptr;         // [ndofs] SpMV input rounded to FP32 (FP32 Jacobian)
   double* part = nullptr;       // partial dot products
-  double* hdev = nullptr;
+  double* hdev = nullptr;       // [kHcol] device: two CGS passes' coefficients + the norm²
+  double* hhost = nullptr;      // [kHcol] pinned host copy of hdev
   int64_t part_len = 0;
   // transposed pattern for the adjoint
   int64_t* rowptrT = nullptr;
@@ -50,18 +52,49 @@ struct Solver {
 
 #define S_CUDA GB_CUDA
 
+// Layout of Solver::hdev / hhost: [0, 256) first Gram–Schmidt pass, [256, 512) second
+// pass, [512] squared norm of the new direction.
+constexpr int kHB = 256, kHN = 512, kHcol = 513;
+
 // ------------------------------------------------------------------ kernels
-template <typename V>
-__global__ void k_spmv(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                       const V* __restrict__ val, const double* __restrict__ x, double* __restrict__ y) {
+// y = A x for the FP32 Jacobian: x arrives rounded to FP32 and the products accumulate in
+// FP32 (per lane, then a warp-shuffle reduction); one conversion per row to the FP64 y.
+// The rounding is of the order of the FP32 matrix values' own.  GB300 issues FP64 at a
+// small fraction of its FP32 rate, and a per-nonzero FP64 convert + FMA made this kernel
+// FP64-bound rather than HBM-bound.
+__global__ void k_spmv_f32(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                           const float* __restrict__ val, const float* __restrict__ x, double* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; row < n;
        row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    double acc = 0.0;
-    for (int64_t t = rowptr[row] + lane; t < rowptr[row + 1]; t += 32) acc += (double)val[t] * x[col[t]];
+    float acc = 0.0f;
+    const int64_t t1 = rowptr[row + 1];
+    for (int64_t t = rowptr[row] + lane; t < t1; t += 32) acc = fmaf(val[t], x[col[t]], acc);
     for (int s = 16; s > 0; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s);
-    if (lane == 0) y[row] = acc;
+    if (lane == 0) y[row] = (double)acc;
   }
+}
+
+// y = A x for the FP64 Jacobian: 8 lanes per row, so a row's reduction takes 3 shuffle
+// steps over 8 lanes instead of 5 over 32 (FP64 issue slots are the scarce resource).
+__global__ void k_spmv_f64(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                           const double* __restrict__ val, const double* __restrict__ x, double* __restrict__ y) {
+  const int sub = threadIdx.x & 7;
+  for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 3; row - ((threadIdx.x & 31) >> 3) < n;
+       row += ((int64_t)gridDim.x * blockDim.x) >> 3) {
+    double acc = 0.0;
+    if (row < n) {
+      const int64_t t1 = rowptr[row + 1];
+      for (int64_t t = rowptr[row] + sub; t < t1; t += 8) acc = fma(val[t], x[col[t]], acc);
+    }
+    for (int s = 4; s > 0; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s, 8);
+    if (sub == 0 && row < n) y[row] = acc;
+  }
+}
+
+__global__ void k_to_f32(int64_t n, const double* __restrict__ x, float* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
 }
 
 // y = Aᵀ x through the transposed pattern (values gathered through perm).
@@ -265,6 +298,16 @@ __global__ void k_scale_copy(int64_t n, double a, const double* __restrict__ x, 
     y[j] = a * x[j];
 }
 
+// y = x / sqrt(*nrm2) when *nrm2 > 0 (the norm stays on the device)
+__global__ void k_scale_rsqrt(int64_t n, const double* __restrict__ nrm2, const double* __restrict__ x,
+                              double* __restrict__ y) {
+  const double q = *nrm2;
+  if (!(q > 0.0)) return;
+  const double a = 1.0 / sqrt(q);
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+    y[j] = a * x[j];
+}
+
 __global__ void k_fz_grad(int64_t ncells, const int32_t* __restrict__ row, const double* __restrict__ lam,
                           const double* __restrict__ fz, double* __restrict__ out) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
@@ -295,13 +338,26 @@ static int dot(gbmhd_ctx* ctx, Solver* s, const double* V, int k1, const double*
   return 0;
 }
 
+// h_dev[i] = V_iᵀ w, i < k1, left on the device (no host round trip).
+static int dot_dev(gbmhd_ctx* ctx, Solver* s, const double* V, int k1, const double* w, double* h_dev) {
+  const int64_t n = ctx->ndofs;
+  const int nb = (int)std::min<int64_t>(std::max<int64_t>(1, (n + 255) / 256), (int64_t)ctx->num_sms * 2);
+  dim3 g(nb, k1);
+  { k_mdot_partial<<<g, 256, 0, ctx->stream>>>(n, k1, V, w, s->part); gbmhd::count_launch(); }
+  { k_mdot_final<<<k1, 256, 0, ctx->stream>>>(k1, nb, s->part, h_dev); gbmhd::count_launch(); }
+  S_CUDA(cudaGetLastError());
+  return 0;
+}
+
 static int spmv(gbmhd_ctx* ctx, int precision, const double* x, double* y) {
   const int64_t n = ctx->ndofs;
-  const int g = grid_for(ctx, n * 32);
-  if (precision == GBMHD_MIXED)
-    { k_spmv<float><<<g, 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val32, x, y); gbmhd::count_launch(); }
-  else
-    { k_spmv<double><<<g, 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val64, x, y); gbmhd::count_launch(); }
+  Solver* s = ctx->solver;
+  if (precision == GBMHD_MIXED) {
+    { k_to_f32<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, x, s->x32); gbmhd::count_launch(); }
+    { k_spmv_f32<<<grid_for(ctx, n * 32), 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val32, s->x32, y); gbmhd::count_launch(); }
+  } else {
+    { k_spmv_f64<<<grid_for(ctx, n * 8), 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val64, x, y); gbmhd::count_launch(); }
+  }
   S_CUDA(cudaGetLastError());
   return 0;
 }
@@ -332,9 +388,11 @@ static int ensure_workspace(gbmhd_ctx* ctx, int m) {
     S_CUDA(cudaMalloc(&s->w, sizeof(double) * n));
     S_CUDA(cudaMalloc(&s->t1, sizeof(double) * n));
     S_CUDA(cudaMalloc(&s->t2, sizeof(double) * n));
+    S_CUDA(cudaMalloc(&s->x32, sizeof(float) * std::max<int64_t>(n, 1)));
     s->part_len = (int64_t)ctx->num_sms * 2 * 257;
     S_CUDA(cudaMalloc(&s->part, sizeof(double) * s->part_len));
-    S_CUDA(cudaMalloc(&s->hdev, sizeof(double) * 257));
+    S_CUDA(cudaMalloc(&s->hdev, sizeof(double) * kHcol));
+    S_CUDA(cudaMallocHost(&s->hhost, sizeof(double) * kHcol));
   }
   return 0;
 }
@@ -482,7 +540,7 @@ static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int
     return r;
   };
   S_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
-  std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), h(m + 2), h2(m + 2);
+  std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), h(m + 2);
   double bnorm = 0.0;
   if ((rc = dot(ctx, s, b, 1, b, &bnorm))) return rc;
   bnorm = std::sqrt(bnorm);
@@ -504,21 +562,19 @@ static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int
       double* zk = s->Z + (int64_t)k * n;
       if ((rc = apply_pc(ctx, precision, vk, zk, transpose))) return rc;
       if ((rc = op(zk, s->w))) return rc;
-      // CGS2
-      if ((rc = dot(ctx, s, s->V, k + 1, s->w, h.data()))) return rc;
-      S_CUDA(cudaMemcpyAsync(s->hdev, h.data(), sizeof(double) * (k + 1), cudaMemcpyHostToDevice, ctx->stream));
+      // CGS2 with the coefficients kept on the device; one host round trip per iteration
+      if ((rc = dot_dev(ctx, s, s->V, k + 1, s->w, s->hdev))) return rc;
       { k_mgs_update<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, k + 1, s->V, s->hdev, s->w); gbmhd::count_launch(); }
-      if ((rc = dot(ctx, s, s->V, k + 1, s->w, h2.data()))) return rc;
-      S_CUDA(cudaMemcpyAsync(s->hdev, h2.data(), sizeof(double) * (k + 1), cudaMemcpyHostToDevice, ctx->stream));
-      { k_mgs_update<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, k + 1, s->V, s->hdev, s->w); gbmhd::count_launch(); }
-      for (int i = 0; i <= k; ++i) h[i] += h2[i];
-      double hn = 0.0;
-      if ((rc = dot(ctx, s, s->w, 1, s->w, &hn))) return rc;
-      hn = std::sqrt(hn);
+      if ((rc = dot_dev(ctx, s, s->V, k + 1, s->w, s->hdev + kHB))) return rc;
+      { k_mgs_update<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, k + 1, s->V, s->hdev + kHB, s->w); gbmhd::count_launch(); }
+      if ((rc = dot_dev(ctx, s, s->w, 1, s->w, s->hdev + kHN))) return rc;
+      { k_scale_rsqrt<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, s->hdev + kHN, s->w, s->V + (int64_t)(k + 1) * n); gbmhd::count_launch(); }
+      S_CUDA(cudaMemcpyAsync(s->hhost, s->hdev, sizeof(double) * kHcol, cudaMemcpyDeviceToHost, ctx->stream));
+      S_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (int i = 0; i <= k; ++i) h[i] = s->hhost[i] + s->hhost[kHB + i];
+      const double hn = std::sqrt(std::max(0.0, s->hhost[kHN]));
       for (int i = 0; i <= k; ++i) H[i * m + k] = h[i];
       H[(k + 1) * m + k] = hn;
-      if (hn > 0.0)
-        { k_scale_copy<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0 / hn, s->w, s->V + (int64_t)(k + 1) * n); gbmhd::count_launch(); }
       for (int i = 0; i < k; ++i) {
         const double t = cs[i] * H[i * m + k] + sn[i] * H[(i + 1) * m + k];
         H[(i + 1) * m + k] = -sn[i] * H[i * m + k] + cs[i] * H[(i + 1) * m + k];
@@ -566,10 +622,11 @@ void solver_destroy(gbmhd_ctx* ctx) {
   Solver* s = ctx->solver;
   if (!s) return;
   mf_destroy(s->mf);
-  void* ptrs[] = {s->Mp_inv, s->Mf_inv, s->seg, s->V, s->Z, s->w, s->t1, s->t2, s->part, s->hdev,
+  void* ptrs[] = {s->Mp_inv, s->Mf_inv, s->seg, s->V, s->Z, s->w, s->t1, s->t2, s->x32, s->part, s->hdev,
                   s->rowptrT, s->colT, s->permT};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (s->hhost) cudaFreeHost(s->hhost);
   delete s;
   ctx->solver = nullptr;
 }
@@ -853,6 +910,16 @@ __global__ void k_zero_non_uj(int64_t n, int64_t pb, int64_t pe, int64_t fb, dou
     const bool uj = j < pb || (j >= pe && j < fb);
     if (!uj) x[j] = 0.0;
   }
+}
+
+extern "C" int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double* bytes_per_apply) {
+  if (!ctx || !applies || !seconds || !bytes_per_apply) return -1;
+  *applies = 0;
+  *seconds = 0.0;
+  *bytes_per_apply = 0.0;
+  if (!ctx->solver || !ctx->solver->mf) return 0;
+  mf_sweep_stats(ctx->solver->mf, applies, seconds, bytes_per_apply);
+  return 0;
 }
 
 extern "C" int gbmhd_diag_uj_solve_error(gbmhd_ctx* ctx, const double* d_state, int32_t precision, double* err) {
