@@ -101,6 +101,7 @@ static int set_params_impl(gbmhd_ctx* ctx, const gbmhd_params* p, bool first) {
 extern "C" int gbmhd_set_params(gbmhd_ctx* ctx, const gbmhd_params* p) {
   if (!ctx) return -1;
   GB_CUDA(cudaStreamSynchronize(ctx->stream));  // no kernel of this context may read the old values
+  ctx->params_gen++;
   return set_params_impl(ctx, p, false);
 }
 

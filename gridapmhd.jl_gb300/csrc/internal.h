@@ -122,6 +122,7 @@ struct gbmhd_ctx {
   double* d_r = nullptr;               // [ndofs] residual work vector
   double* d_xtmp = nullptr;            // [ndofs]
   struct Solver* solver = nullptr;     // linear-solver workspace (solver.cu)
+  int64_t params_gen = 0;              // incremented by every gbmhd_set_params
 };
 
 // assemble.cu

@@ -76,4 +76,7 @@ int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, int values, const dou
 // b is overwritten in those entries.
 int mf_solve(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transpose);
 void mf_destroy(MFNumeric* M);
+// Solves timed since the last call (CUDA events on the context stream), their total
+// device time, and the factor bytes one solve reads; resets the counters.
+void mf_sweep_stats(MFNumeric* M, int64_t* applies, double* seconds, double* bytes_per_apply);
 int mf_precision(const MFNumeric* M);

@@ -108,7 +108,14 @@ static int upload(gbmhd_ctx* ctx, V** dst, const std::vector<V>& src) {
 }
 
 int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
-  // the solve sweeps stage a front's vector segment in shared memory
+  // the solve sweeps stage a front's vector segment in shared memory and read fronts with
+  // 16-byte vector loads: every front must start on a multiple of 8 entries with n % 8 == 0
+  for (const MFLevel& L : S.levels)
+    if (L.E % 8 || L.n % 8 || L.off % 64) {
+      ctx->err = "multifrontal: front sizes are not padded to multiples of 8";
+      *out = nullptr;
+      return -1;
+    }
   for (const MFLevel& L : S.levels)
     if (sizeof(double) * (size_t)L.n > 200 * 1024) {
       ctx->err = "multifrontal: front of " + std::to_string(L.n) + " dofs exceeds the solve kernels' staging limit";
@@ -225,114 +232,225 @@ __global__ void k_extend_add(T* F, const int32_t* __restrict__ child_list, int64
   }
 }
 
-// Inverse of the kb x kb pivot block of every front (Gauss-Jordan with partial
-// pivoting inside the block), computed in FP64 whatever the storage type and then
-// rounded to it.  P[f] (NB x NB, column-major, ld NB).
+// Inverse of the kb x kb pivot block of every front: in-place Gauss-Jordan with partial
+// pivoting inside the block (row interchanges, undone as column interchanges at the end),
+// computed in FP64 whatever the storage type and then rounded to it.  kb³ FP64 multiply-
+// adds per block; the pivot search is one warp's shuffle argmax.  P[f] (NB x NB,
+// column-major, ld NB, zero outside kb x kb).
 template <typename T>
 __global__ void __launch_bounds__(256) k_pivot_inverse(const T* __restrict__ F, int64_t off, int n, int k, int kb,
                                                        T* __restrict__ P, int32_t* err) {
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  double* A = reinterpret_cast<double*>(sm_raw);  // kb x 2kb, row-major [i][j]
+  __shared__ double A[NB * NB];  // column-major, ld kb
+  __shared__ double rowc[NB], mcol[NB];
+  __shared__ int perm[NB], colsrc[NB];
   __shared__ int piv_row;
-  __shared__ double piv_abs[256];
-  __shared__ int piv_idx[256];
   const int64_t f = blockIdx.x;
   const T* M = F + off + f * (int64_t)n * n;
-  const int w = 2 * kb;
-  for (int idx = threadIdx.x; idx < kb * w; idx += blockDim.x) {
-    const int i = idx / w, j = idx % w;
-    A[idx] = j < kb ? (double)M[(k + i) + (int64_t)(k + j) * n] : ((j - kb) == i ? 1.0 : 0.0);
-  }
+  const int tid = threadIdx.x;
+  const int ti = tid & (NB - 1), tj = tid / NB;  // row, first column of this thread (4 column groups)
+  constexpr int CG = 256 / NB;
+  if (ti < kb)
+    for (int j = tj; j < kb; j += CG) A[ti + j * kb] = (double)M[(k + ti) + (int64_t)(k + j) * n];
   __syncthreads();
   for (int c = 0; c < kb; ++c) {
-    // pivot search in column c, rows c..kb-1
-    double best = -1.0;
-    int bi = c;
-    for (int i = c + threadIdx.x; i < kb; i += blockDim.x) {
-      const double a = fabs((double)A[i * w + c]);
-      if (a > best) { best = a; bi = i; }
-    }
-    piv_abs[threadIdx.x] = best;
-    piv_idx[threadIdx.x] = bi;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s && piv_abs[threadIdx.x + s] > piv_abs[threadIdx.x]) {
-        piv_abs[threadIdx.x] = piv_abs[threadIdx.x + s];
-        piv_idx[threadIdx.x] = piv_idx[threadIdx.x + s];
+    if (tid < 32) {  // argmax |A[i, c]| over rows c..kb-1 (ties: the lower row)
+      double best = -1.0;
+      int bi = c;
+      for (int i = c + tid; i < kb; i += 32) {
+        const double a = fabs(A[i + c * kb]);
+        if (a > best) { best = a; bi = i; }
       }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      piv_row = piv_idx[0];
-      if (!(piv_abs[0] > 0.0)) atomicExch(err, 1);
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (tid == 0) {
+        piv_row = bi;
+        perm[c] = bi;
+        if (!(best > 0.0)) atomicExch(err, 1);
+      }
     }
     __syncthreads();
     const int pr = piv_row;
-    if (pr != c)
-      for (int j = threadIdx.x; j < w; j += blockDim.x) {
-        const double t = A[c * w + j];
-        A[c * w + j] = A[pr * w + j];
-        A[pr * w + j] = t;
-      }
+    if (pr != c && tid < kb) {
+      const double t = A[c + tid * kb];
+      A[c + tid * kb] = A[pr + tid * kb];
+      A[pr + tid * kb] = t;
+    }
     __syncthreads();
-    const double d = A[c * w + c];
-    const double inv = d != 0.0 ? 1.0 / d : 0.0;
+    if (tid < kb) {
+      const double d = A[c + c * kb];
+      const double inv = d != 0.0 ? 1.0 / d : 0.0;
+      rowc[tid] = tid == c ? inv : A[c + tid * kb] * inv;
+      mcol[tid] = tid == c ? 0.0 : A[tid + c * kb];
+    }
     __syncthreads();
-    for (int j = threadIdx.x; j < w; j += blockDim.x) A[c * w + j] *= inv;
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < kb * w; idx += blockDim.x) {
-      const int i = idx / w, j = idx % w;
-      if (i != c) {
-        const double m = A[i * w + c];
-        if (m != 0.0 && j != c) A[idx] -= m * A[c * w + j];
+    if (ti < kb) {
+      const double mi = mcol[ti];
+      for (int j = tj; j < kb; j += CG) {
+        const int idx = ti + j * kb;
+        A[idx] = ti == c ? rowc[j] : (j == c ? 0.0 : A[idx]) - mi * rowc[j];
       }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < kb; i += blockDim.x)
-      if (i != c) A[i * w + c] = 0.0;
-    __syncthreads();
   }
+  if (tid == 0) {  // undo the row interchanges as column interchanges, last first
+    for (int j = 0; j < kb; ++j) colsrc[j] = j;
+    for (int c = kb - 1; c >= 0; --c) {
+      const int p = perm[c];
+      const int t = colsrc[c];
+      colsrc[c] = colsrc[p];
+      colsrc[p] = t;
+    }
+  }
+  __syncthreads();
   T* Pf = P + f * (int64_t)NB * NB;
-  for (int idx = threadIdx.x; idx < NB * NB; idx += blockDim.x) {
-    const int i = idx % NB, j = idx / NB;  // column-major
-    Pf[idx] = (i < kb && j < kb) ? (T)A[i * w + kb + j] : (T)0;
-  }
+  for (int j = tj; j < NB; j += CG)  // column-major, zero outside kb x kb
+    Pf[ti + j * NB] = (ti < kb && j < kb) ? (T)A[ti + colsrc[j] * kb] : (T)0;
 }
 
-// C = M[:, K] with the K rows zeroed; Tb = M[K, :]  (both per front).
+// The same in-place Gauss-Jordan for FP32 factors, in float-float arithmetic on the FP32
+// pipes (~48 significant bits; the result is rounded to FP32).  GB300 issues FP64 at a
+// small fraction of its FP32 rate: the kb³ updates cost ~14 FP32 operations each here
+// instead of one FP64 FMA, which is still several times faster.  The per-column scalars
+// (the pivot's reciprocal, the scaled pivot row) are formed in FP64.
+__device__ __forceinline__ void df_split(double x, float& h, float& l) {
+  h = (float)x;
+  l = (float)(x - (double)h);
+}
+
+__global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restrict__ F, int64_t off, int n, int k,
+                                                          int kb, float* __restrict__ P, int32_t* err) {
+  __shared__ float Ah[NB * NB], Al[NB * NB];  // column-major, ld kb
+  __shared__ float rh[NB], rl[NB], mh[NB], ml[NB];
+  __shared__ int perm[NB], colsrc[NB];
+  __shared__ int piv_row;
+  const int64_t f = blockIdx.x;
+  const float* M = F + off + f * (int64_t)n * n;
+  const int tid = threadIdx.x;
+  const int ti = tid & (NB - 1), tj = tid / NB;  // row, first column of this thread (4 column groups)
+  constexpr int CG = 256 / NB;
+  if (ti < kb)
+    for (int j = tj; j < kb; j += CG) {
+      Ah[ti + j * kb] = M[(k + ti) + (int64_t)(k + j) * n];
+      Al[ti + j * kb] = 0.0f;
+    }
+  __syncthreads();
+  for (int c = 0; c < kb; ++c) {
+    if (tid < 32) {  // argmax |A[i, c]| over rows c..kb-1 (ties: the lower row)
+      double best = -1.0;
+      int bi = c;
+      for (int i = c + tid; i < kb; i += 32) {
+        const double a = fabs((double)Ah[i + c * kb] + (double)Al[i + c * kb]);
+        if (a > best) { best = a; bi = i; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (tid == 0) {
+        piv_row = bi;
+        perm[c] = bi;
+        if (!(best > 0.0)) atomicExch(err, 1);
+      }
+    }
+    __syncthreads();
+    const int pr = piv_row;
+    if (pr != c && tid < kb) {
+      float t = Ah[c + tid * kb];
+      Ah[c + tid * kb] = Ah[pr + tid * kb];
+      Ah[pr + tid * kb] = t;
+      t = Al[c + tid * kb];
+      Al[c + tid * kb] = Al[pr + tid * kb];
+      Al[pr + tid * kb] = t;
+    }
+    __syncthreads();
+    if (tid < kb) {
+      const double d = (double)Ah[c + c * kb] + (double)Al[c + c * kb];
+      const double inv = d != 0.0 ? 1.0 / d : 0.0;
+      const double r = tid == c ? inv : ((double)Ah[c + tid * kb] + (double)Al[c + tid * kb]) * inv;
+      df_split(r, rh[tid], rl[tid]);
+      if (tid == c) { mh[tid] = 0.0f; ml[tid] = 0.0f; }
+      else { mh[tid] = Ah[tid + c * kb]; ml[tid] = Al[tid + c * kb]; }
+    }
+    __syncthreads();
+    if (ti < kb) {
+      const float m_h = mh[ti], m_l = ml[ti];
+      for (int j = tj; j < kb; j += CG) {
+        const int idx = ti + j * kb;
+        if (ti == c) {
+          Ah[idx] = rh[j];
+          Al[idx] = rl[j];
+          continue;
+        }
+        const float ah = j == c ? 0.0f : Ah[idx], al = j == c ? 0.0f : Al[idx];
+        // p = m · r in float-float
+        const float r_h = rh[j], r_l = rl[j];
+        const float ph = __fmul_rn(m_h, r_h);
+        float pl = fmaf(m_h, r_h, -ph);
+        pl = fmaf(m_h, r_l, pl);
+        pl = fmaf(m_l, r_h, pl);
+        // a − p: TwoSum on the high parts, the low parts added to the error, renormalised by TwoSum
+        const float sh = __fsub_rn(ah, ph);
+        const float bv = __fsub_rn(sh, ah);
+        const float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(sh, bv)), __fsub_rn(-ph, bv));
+        const float sl = __fadd_rn(e, __fsub_rn(al, pl));
+        const float h = __fadd_rn(sh, sl);
+        const float hv = __fsub_rn(h, sh);
+        Ah[idx] = h;
+        Al[idx] = __fadd_rn(__fsub_rn(sh, __fsub_rn(h, hv)), __fsub_rn(sl, hv));
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {  // undo the row interchanges as column interchanges, last first
+    for (int j = 0; j < kb; ++j) colsrc[j] = j;
+    for (int c = kb - 1; c >= 0; --c) {
+      const int p = perm[c];
+      const int t = colsrc[c];
+      colsrc[c] = colsrc[p];
+      colsrc[p] = t;
+    }
+  }
+  __syncthreads();
+  float* Pf = P + f * (int64_t)NB * NB;
+  for (int j = tj; j < NB; j += CG)  // column-major, zero outside kb x kb
+    Pf[ti + j * NB] = (ti < kb && j < kb) ? __fadd_rn(Ah[ti + colsrc[j] * kb], Al[ti + colsrc[j] * kb]) : 0.0f;
+}
+
+// C = M[0:w, K] with the K rows zeroed; Tb = M[K, 0:w]  (both per front; w = E: the
+// Gauss-Jordan sweep runs over the pivot block F11 only).  Grid (column groups, fronts).
 template <typename T>
-__global__ void k_gj_copy(const T* __restrict__ F, int64_t off, int n, int k, int kb, T* __restrict__ C,
-                          T* __restrict__ Tb) {
+__global__ void __launch_bounds__(256) k_gj_copy(const T* __restrict__ F, int64_t off, int n, int w, int k, int kb,
+                                                 T* __restrict__ C, T* __restrict__ Tb) {
   const int64_t f = blockIdx.y;
   const T* M = F + off + f * (int64_t)n * n;
   T* Cf = C + f * (int64_t)n * NB;
   T* Tf = Tb + f * (int64_t)NB * n;
-  const int64_t tot = (int64_t)n * kb;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < tot; idx += (int64_t)gridDim.x * blockDim.x) {
-    // column block: idx = i + j*n
-    const int i = (int)(idx % n), j = (int)(idx / n);
-    const T v = M[i + (int64_t)(k + j) * n];
-    Cf[i + (int64_t)j * n] = (i >= k && i < k + kb) ? (T)0 : v;
-    // row block: idx = r + c*kb
-    const int r = (int)(idx % kb), c = (int)(idx / kb);
-    Tf[r + (int64_t)c * NB] = M[(k + r) + (int64_t)c * n];
-  }
+  for (int j = blockIdx.x; j < kb; j += gridDim.x)  // C: w rows of column k + j
+    for (int i = threadIdx.x; i < w; i += blockDim.x)
+      Cf[i + (int64_t)j * n] = (i >= k && i < k + kb) ? (T)0 : M[i + (int64_t)(k + j) * n];
+  const int r = threadIdx.x & (NB - 1);
+  for (int c = blockIdx.x * (256 / NB) + threadIdx.x / NB; c < w; c += gridDim.x * (256 / NB))  // Tb: kb rows
+    if (r < kb) Tf[r + (int64_t)c * NB] = M[(k + r) + (int64_t)c * n];
 }
 
-// M[K, j] = T2[:, j] for j outside K; M[K, K] = P.
+// M[K, c] = T2[:, c] for c < w outside K; M[K, K] = P.
 template <typename T>
-__global__ void k_gj_fix(T* __restrict__ F, int64_t off, int n, int k, int kb, const T* __restrict__ T2,
-                         const T* __restrict__ P) {
+__global__ void __launch_bounds__(256) k_gj_fix(T* __restrict__ F, int64_t off, int n, int w, int k, int kb,
+                                                const T* __restrict__ T2, const T* __restrict__ P) {
   const int64_t f = blockIdx.y;
   T* M = F + off + f * (int64_t)n * n;
   const T* T2f = T2 + f * (int64_t)NB * n;
   const T* Pf = P + f * (int64_t)NB * NB;
-  const int64_t tot = (int64_t)n * kb;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < tot; idx += (int64_t)gridDim.x * blockDim.x) {
-    const int r = (int)(idx % kb), c = (int)(idx / kb);
-    const bool inK = c >= k && c < k + kb;
-    M[(k + r) + (int64_t)c * n] = inK ? Pf[r + (int64_t)(c - k) * NB] : T2f[r + (int64_t)c * NB];
-  }
+  const int r = threadIdx.x & (NB - 1);
+  for (int c = blockIdx.x * (256 / NB) + threadIdx.x / NB; c < w; c += gridDim.x * (256 / NB))
+    if (r < kb) {
+      const bool inK = c >= k && c < k + kb;
+      M[(k + r) + (int64_t)c * n] = inK ? Pf[r + (int64_t)(c - k) * NB] : T2f[r + (int64_t)c * NB];
+    }
 }
 
 // ------------------------------------------------------------------ solve kernels
@@ -373,6 +491,7 @@ struct SweepAcc<float> {
     hi = s;
     lo = __fadd_rn(lo, __fadd_rn(err, pe));
   }
+  __device__ void merge(const SweepAcc<float>& o) { merge(o.hi, o.lo); }
   __device__ void merge(float ohi, float olo) {
     const float s = __fadd_rn(hi, ohi);
     const float bp = __fsub_rn(s, hi);
@@ -395,11 +514,56 @@ struct SweepAcc<double> {
   double a = 0.0;
   __device__ static V pack(double t) { return t; }
   __device__ void add(double m, V v) { a = fma(m, v, a); }
+  __device__ void merge(const SweepAcc<double>& o) { a += o.a; }
   __device__ void warp_reduce() {
     for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
   }
   __device__ double value() const { return a; }
 };
+
+// 16-byte vectors of factor entries: a thread of the chunked sweeps owns R consecutive
+// rows (column-major fronts: one vector load per column).
+template <typename T>
+struct RowVec;
+template <>
+struct RowVec<float> {
+  using type = float4;
+  static constexpr int R = 4;
+};
+template <>
+struct RowVec<double> {
+  using type = double2;
+  static constexpr int R = 2;
+};
+
+// acc[r] += Σ_{k<len} col[k·ld + r] · v[k], r < R: eight 16-byte loads in flight per
+// thread, R independent accumulators.  col must be 16-byte aligned and ld a multiple of R.
+template <typename T>
+__device__ __forceinline__ void strided_dot_rows(SweepAcc<T> (&acc)[RowVec<T>::R], const T* __restrict__ col,
+                                                 int64_t ld, const typename SweepAcc<T>::V* __restrict__ v, int len) {
+  using VT = typename RowVec<T>::type;
+  constexpr int R = RowVec<T>::R;
+  int k = 0;
+  for (; k + 8 <= len; k += 8) {
+    VT q[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) q[u] = __ldcs(reinterpret_cast<const VT*>(col + (int64_t)(k + u) * ld));
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const T* qa = reinterpret_cast<const T*>(&q[u]);
+      const typename SweepAcc<T>::V vv = v[k + u];
+#pragma unroll
+      for (int r = 0; r < R; ++r) acc[r].add(qa[r], vv);
+    }
+  }
+  for (; k < len; ++k) {
+    const VT q = __ldcs(reinterpret_cast<const VT*>(col + (int64_t)k * ld));
+    const T* qa = reinterpret_cast<const T*>(&q);
+    const typename SweepAcc<T>::V vv = v[k];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r].add(qa[r], vv);
+  }
+}
 
 // Transposed sweeps (adjoint solves), one warp per column: each dot product runs down a
 // contiguous column of the column-major front.
@@ -458,72 +622,79 @@ __global__ void __launch_bounds__(256) k_bwd_gemv_t(const T* __restrict__ F, con
   if (lane == 0) x[elim[elim_ptr[f] + i]] = acc.value();
 }
 
-// Chunked sweeps: grid (row tiles, column chunks, fronts); each thread owns one row of its
-// tile and reduces one chunk of `cols` columns, staged in shared memory; partial sums are
-// added atomically.  Row accesses are coalesced (column-major fronts).  The chunk width is
-// chosen per level so that levels with few fronts still fill the GPU.
-constexpr int SW_ROWS = 128;  // rows per CTA (one per thread)
+// Chunked sweeps: grid (row tiles, column chunks, fronts); each thread owns R consecutive
+// rows of its tile and reduces one chunk of `cols` columns, staged in shared memory; partial
+// sums are added atomically.  Row accesses are coalesced 16-byte vectors (column-major
+// fronts; E, B and n are multiples of 8, so every vector is aligned and rows up to the next
+// multiple of R stay inside the padded front).  The chunk width is chosen per level so that
+// levels with few fronts still fill the GPU.
+constexpr int SW_THREADS = 128;
 
 // forward: b[bnd_j] += Σ_{i<ne} M[E+j, i] t_i
 template <typename T>
-__global__ void __launch_bounds__(SW_ROWS) k_fwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                       double* __restrict__ b, const double* __restrict__ tsave,
-                                                       const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
-                                                       const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_nb,
-                                                       const int32_t* __restrict__ f_ne, int64_t first, int n, int E,
-                                                       int cols) {
+__global__ void __launch_bounds__(SW_THREADS) k_fwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                          double* __restrict__ b, const double* __restrict__ tsave,
+                                                          const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
+                                                          const int64_t* __restrict__ bnd_ptr,
+                                                          const int32_t* __restrict__ f_nb,
+                                                          const int32_t* __restrict__ f_ne, int64_t first, int n, int E,
+                                                          int cols) {
   using V = typename SweepAcc<T>::V;
+  constexpr int R = RowVec<T>::R;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   V* ts = reinterpret_cast<V*>(sm_raw);
   const int64_t f = first + blockIdx.z;
   const int nb = f_nb[f];
-  const int j = blockIdx.x * SW_ROWS + threadIdx.x;
+  const int j0 = (blockIdx.x * SW_THREADS + threadIdx.x) * R;
   const int ne = f_ne[f];  // columns [ne, E) are padding
   const int c0 = blockIdx.y * cols, c1 = min(ne, c0 + cols);
-  if (blockIdx.x * SW_ROWS >= nb || c0 >= ne) return;
+  if (blockIdx.x * SW_THREADS * R >= nb || c0 >= ne) return;
   const double* t = tsave + toff[f];
   for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = SweepAcc<T>::pack(t[c]);
   __syncthreads();
-  if (j >= nb) return;
-  const T* M = F + f_off[f] + E + j;
-  SweepAcc<T> acc;
-#pragma unroll 8
-  for (int c = c0; c < c1; ++c) acc.add(M[(int64_t)c * n], ts[c - c0]);
-  atomicAdd(&b[bnd[bnd_ptr[f] + j]], acc.value());
+  if (j0 >= nb) return;
+  SweepAcc<T> acc[R];
+  strided_dot_rows<T>(acc, F + f_off[f] + E + j0 + (int64_t)c0 * n, n, ts, c1 - c0);
+  const int32_t* bd = bnd + bnd_ptr[f];
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (j0 + r < nb) atomicAdd(&b[bd[j0 + r]], acc[r].value());
 }
 
 // backward: y_i = Σ_c M[i, c] v_c with v = [t ; −x_B], accumulated into ybuf (then scattered)
 template <typename T>
-__global__ void __launch_bounds__(SW_ROWS) k_bwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                       const double* __restrict__ x, const double* __restrict__ tsave,
-                                                       const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
-                                                       const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
-                                                       const int32_t* __restrict__ f_nb, double* __restrict__ ybuf,
-                                                       int64_t first, int n, int E, int cols) {
+__global__ void __launch_bounds__(SW_THREADS) k_bwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                          const double* __restrict__ x, const double* __restrict__ tsave,
+                                                          const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
+                                                          const int64_t* __restrict__ bnd_ptr,
+                                                          const int32_t* __restrict__ f_ne,
+                                                          const int32_t* __restrict__ f_nb, double* __restrict__ ybuf,
+                                                          int64_t first, int n, int E, int cols) {
   using V = typename SweepAcc<T>::V;
+  constexpr int R = RowVec<T>::R;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   V* vs = reinterpret_cast<V*>(sm_raw);
   const int64_t f = first + blockIdx.z;
   const int ne = f_ne[f], nb = f_nb[f];
-  const int i = blockIdx.x * SW_ROWS + threadIdx.x;
+  const int i0 = (blockIdx.x * SW_THREADS + threadIdx.x) * R;
   // virtual columns v in [0, ne + nb): v < ne -> column v, else column E + (v − ne)
   const int c0 = blockIdx.y * cols, c1 = min(ne + nb, c0 + cols);
-  if (blockIdx.x * SW_ROWS >= ne || c0 >= ne + nb) return;
+  if (blockIdx.x * SW_THREADS * R >= ne || c0 >= ne + nb) return;
   const double* t = tsave + toff[f];
   const int32_t* bd = bnd + bnd_ptr[f];
   for (int v = c0 + threadIdx.x; v < c1; v += blockDim.x)
     vs[v - c0] = SweepAcc<T>::pack(v < ne ? t[v] : -x[bd[v - ne]]);
   __syncthreads();
-  if (i >= ne) return;
-  const T* M = F + f_off[f] + i;
-  SweepAcc<T> acc;
+  if (i0 >= ne) return;
+  const T* M = F + f_off[f] + i0;
+  SweepAcc<T> acc[R];
   const int va = min(c1, ne);
-#pragma unroll 8
-  for (int v = c0; v < va; ++v) acc.add(M[(int64_t)v * n], vs[v - c0]);
-  const T* MB = M + (int64_t)(E - ne) * n;
-#pragma unroll 8
-  for (int v = max(c0, ne); v < c1; ++v) acc.add(MB[(int64_t)v * n], vs[v - c0]);
-  atomicAdd(&ybuf[toff[f] + i], acc.value());
+  if (va > c0) strided_dot_rows<T>(acc, M + (int64_t)c0 * n, n, vs, va - c0);
+  const int vb = max(c0, ne);  // boundary columns: virtual v -> column E + (v − ne)
+  if (c1 > vb) strided_dot_rows<T>(acc, M + (int64_t)(E - ne + vb) * n, n, vs + (vb - c0), c1 - vb);
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (i0 + r < ne) atomicAdd(&ybuf[toff[f] + i0 + r], acc[r].value());
 }
 
 __global__ void k_bwd_scatter(double* __restrict__ x, double* __restrict__ ybuf, const int64_t* __restrict__ toff,
@@ -627,15 +798,18 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
                                                      M->d.f_parent, M->d.f_level, M->d.ea_ptr, M->d.ea_pos, d_ln, d_le); gbmhd::count_launch(); }
     }
     MF_CUDA(cudaGetLastError());
+    // Blocked in-place Gauss-Jordan over the eliminated pivots: every 64-pivot step updates
+    // the whole front, so F12, F21 and S are formed by the same progressive elimination as
+    // F11⁻¹.  (Forming them afterwards from the FP32 F11⁻¹ with three large GEMMs multiplies
+    // the inverse's rounding by κ(F11): at Ha = 500 that tripled the FGMRES iterations.)
     for (int k = 0; k < E; k += NB) {
       const int kb = std::min(NB, E - k);
-      const size_t sm = sizeof(double) * (size_t)kb * 2 * kb;
-      auto kinv = k_pivot_inverse<T>;
-      MF_CUDA(cudaFuncSetAttribute(kinv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(double) * NB * 2 * NB)));
-      { kinv<<<cnt, 256, sm, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
-      const int64_t tot = (int64_t)n * kb;
-      dim3 gc((unsigned)std::min<int64_t>((tot + 255) / 256, 1024), (unsigned)cnt);
-      { k_gj_copy<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, C, Tb); gbmhd::count_launch(); }
+      if constexpr (sizeof(T) == 4)
+        { k_pivot_inverse_df<<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
+      else
+        { k_pivot_inverse<T><<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
+      dim3 gc((unsigned)std::max(kb, (n + 3) / 4), (unsigned)cnt);
+      { k_gj_copy<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, n, k, kb, C, Tb); gbmhd::count_launch(); }
       MF_CUDA(cudaGetLastError());
       // T2 = P · Tb  (kb x n)
       gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, kb, n, kb, &one, P, NB, (long long)NB * NB, Tb, NB,
@@ -646,7 +820,7 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
       // M[:, K] = −C · P  (n x kb)
       gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, kb, kb, &mone, C, n, (long long)n * NB, P, NB,
                          (long long)NB * NB, &zero, F + L.off + (int64_t)k * n, n, (long long)n * n, cnt));
-      { k_gj_fix<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, T2, P); gbmhd::count_launch(); }
+      { k_gj_fix<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, n, k, kb, T2, P); gbmhd::count_launch(); }
       MF_CUDA(cudaGetLastError());
     }
   }
@@ -677,8 +851,8 @@ int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, int values, const dou
 // Column chunk of the chunked sweeps: wide enough that the partial-sum atomics stay a
 // small fraction of the factor reads, narrow enough that a level with few fronts still
 // launches about two waves of CTAs.
-static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t fronts) {
-  const int64_t per_chunk = std::max<int64_t>(1, (rows + SW_ROWS - 1) / SW_ROWS) * std::max<int64_t>(1, fronts);
+static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t fronts, int rows_per_cta) {
+  const int64_t per_chunk = std::max<int64_t>(1, (rows + rows_per_cta - 1) / rows_per_cta) * std::max<int64_t>(1, fronts);
   const int64_t want = (int64_t)ctx->num_sms * 32;  // 2 waves of 16 resident 128-thread CTAs
   const int64_t chunks = std::max<int64_t>(1, (want + per_chunk - 1) / per_chunk);
   int64_t cols = (ncols + chunks - 1) / chunks;
@@ -689,6 +863,7 @@ static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t
 template <typename T>
 static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool tr) {
   using V = typename SweepAcc<T>::V;
+  const int rows_cta = SW_THREADS * RowVec<T>::R;
   const MFSymbolic& S = M->S;
   const T* F = reinterpret_cast<const T*>(M->F);
   for (size_t l = 0; l < S.levels.size(); ++l) {
@@ -697,9 +872,9 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first, L.E); gbmhd::count_launch(); }
     if (L.B > 0) {
       if (!tr) {
-        const int cols = sweep_cols(ctx, L.B, L.E, cnt);
-        dim3 g((unsigned)((L.B + SW_ROWS - 1) / SW_ROWS), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
-        { k_fwd_chunk<T><<<g, SW_ROWS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
+        const int cols = sweep_cols(ctx, L.B, L.E, cnt, rows_cta);
+        dim3 g((unsigned)((L.B + rows_cta - 1) / rows_cta), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
+        { k_fwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
       } else {
         const size_t sm = sizeof(V) * L.E;
         auto kf = k_fwd_gemv_t<T>;
@@ -714,9 +889,9 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count;
     if (!tr) {
-      const int cols = sweep_cols(ctx, L.E, L.n, cnt);
-      dim3 g((unsigned)((L.E + SW_ROWS - 1) / SW_ROWS), (unsigned)((L.n + cols - 1) / cols), (unsigned)cnt);
-      { k_bwd_chunk<T><<<g, SW_ROWS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
+      const int cols = sweep_cols(ctx, L.E, L.n, cnt, rows_cta);
+      dim3 g((unsigned)((L.E + rows_cta - 1) / rows_cta), (unsigned)((L.n + cols - 1) / cols), (unsigned)cnt);
+      { k_bwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
       { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
     } else {
       const size_t sm = sizeof(V) * L.n;

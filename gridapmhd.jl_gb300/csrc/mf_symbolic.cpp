@@ -249,7 +249,10 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
       L.B = std::max<int32_t>(L.B, (int32_t)bnd[v].size());
       fid[v] = (int32_t)nf++;
     }
-    L.E = std::max(L.E, 1);
+    // padded to multiples of 8 so that every front column starts 32-byte aligned: cuBLAS
+    // then runs its tensor-core kernels (an odd leading dimension falls back to SIMT ones)
+    L.E = (std::max(L.E, 1) + 7) / 8 * 8;
+    L.B = (L.B + 7) / 8 * 8;
     L.n = L.E + L.B;
     L.off = off;
     off += L.count * (int64_t)L.n * L.n;

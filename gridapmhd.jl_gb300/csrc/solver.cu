@@ -45,9 +45,11 @@ struct Solver {
   double* hhost = nullptr;      // [kHcol] pinned host copy of hdev
   int64_t part_len = 0;
   // transposed pattern for the adjoint
-  int64_t* rowptrT = nullptr;
-  int32_t* colT = nullptr;
+  // transposed Jacobian for the adjoint: the pattern is structurally symmetric, so Aᵀ
+  // shares rowptr/col and only the values move: valT[t] = val[permT[t]]
   int64_t* permT = nullptr;
+  double* valT = nullptr;
+  int64_t factor_gen = -1;      // ctx->params_gen when the factors were computed
 };
 
 #define S_CUDA GB_CUDA
@@ -77,10 +79,10 @@ __global__ void k_spmv_f32(int64_t n, const int64_t* __restrict__ rowptr, const 
 
 // y = A x for the FP64 Jacobian: 8 lanes per row, so a row's reduction takes 3 shuffle
 // steps over 8 lanes instead of 5 over 32 (FP64 issue slots are the scarce resource).
-__global__ void k_spmv_f64(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+__global__ void k_spmv_f64(int64_t r0, int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                            const double* __restrict__ val, const double* __restrict__ x, double* __restrict__ y) {
   const int sub = threadIdx.x & 7;
-  for (int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 3; row - ((threadIdx.x & 31) >> 3) < n;
+  for (int64_t row = r0 + ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 3); row - ((threadIdx.x & 31) >> 3) < n;
        row += ((int64_t)gridDim.x * blockDim.x) >> 3) {
     double acc = 0.0;
     if (row < n) {
@@ -97,22 +99,33 @@ __global__ void k_to_f32(int64_t n, const double* __restrict__ x, float* __restr
     y[i] = (float)x[i];
 }
 
-// y = Aᵀ x through the transposed pattern (values gathered through perm).
-template <typename V>
-__global__ void k_spmv_t(int64_t r0, int64_t r1, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                         const int64_t* __restrict__ perm, const V* __restrict__ val, const double* __restrict__ x,
-                         double* __restrict__ y) {
+// permT[t] = position of the entry (col[t], row(t)) in row col[t] (binary search in the
+// sorted row); err = 1 if the pattern is not structurally symmetric.
+__global__ void k_transpose_map(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                                int64_t* __restrict__ permT, int32_t* err) {
   const int lane = threadIdx.x & 31;
-  for (int64_t row = r0 + ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5); row < r1;
-       row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    double acc = 0.0;
-    for (int64_t t = rowptr[row] + lane; t < rowptr[row + 1]; t += 32) acc += (double)val[perm[t]] * x[col[t]];
-    for (int s = 16; s > 0; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s);
-    if (lane == 0) y[row] = acc;
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < n;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    for (int64_t t = rowptr[r] + lane; t < rowptr[r + 1]; t += 32) {
+      const int32_t c = col[t];
+      int64_t lo = rowptr[c], hi = rowptr[c + 1];
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (col[mid] < r) lo = mid + 1;
+        else hi = mid;
+      }
+      if (lo < rowptr[c + 1] && col[lo] == r) permT[t] = lo;
+      else { permT[t] = t; atomicExch(err, 1); }
+    }
   }
 }
 
-// y[row] -= Σ_{p/φ segment} A[row,c] z[c] for the (u,j) rows.
+__global__ void k_gather_vals(int64_t nnz, const double* __restrict__ val, const int64_t* __restrict__ perm,
+                              double* __restrict__ out) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nnz; t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = val[perm[t]];
+}
+
 template <typename V>
 __global__ void k_coupling(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                            const V* __restrict__ val, const int32_t* __restrict__ seg, const double* __restrict__ z,
@@ -356,19 +369,17 @@ static int spmv(gbmhd_ctx* ctx, int precision, const double* x, double* y) {
     { k_to_f32<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, x, s->x32); gbmhd::count_launch(); }
     { k_spmv_f32<<<grid_for(ctx, n * 32), 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val32, s->x32, y); gbmhd::count_launch(); }
   } else {
-    { k_spmv_f64<<<grid_for(ctx, n * 8), 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, ctx->d_val64, x, y); gbmhd::count_launch(); }
+    { k_spmv_f64<<<grid_for(ctx, n * 8), 256, 0, ctx->stream>>>(0, n, ctx->d_rowptr, ctx->d_col, ctx->d_val64, x, y); gbmhd::count_launch(); }
   }
   S_CUDA(cudaGetLastError());
   return 0;
 }
 
-static int spmv_t(gbmhd_ctx* ctx, Solver* s, int precision, int64_t r0, int64_t r1, const double* x, double* y) {
-  const int g = grid_for(ctx, (r1 - r0) * 32);
+// y[r0:r1) = (Aᵀ x)[r0:r1) with the FP64 transposed values (built by prepare_transpose).
+static int spmv_t(gbmhd_ctx* ctx, Solver* s, int64_t r0, int64_t r1, const double* x, double* y) {
   if (r1 <= r0) return 0;
-  if (precision == GBMHD_MIXED)
-    { k_spmv_t<float><<<g, 256, 0, ctx->stream>>>(r0, r1, s->rowptrT, s->colT, s->permT, ctx->d_val32, x, y); gbmhd::count_launch(); }
-  else
-    { k_spmv_t<double><<<g, 256, 0, ctx->stream>>>(r0, r1, s->rowptrT, s->colT, s->permT, ctx->d_val64, x, y); gbmhd::count_launch(); }
+  if (!s->valT) { ctx->err = "transposed operator not prepared"; return -1; }
+  { k_spmv_f64<<<grid_for(ctx, (r1 - r0) * 8), 256, 0, ctx->stream>>>(r0, r1, ctx->d_rowptr, ctx->d_col, s->valT, x, y); gbmhd::count_launch(); }
   S_CUDA(cudaGetLastError());
   return 0;
 }
@@ -477,6 +488,7 @@ static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
   }
   int rc = mf_factor(ctx, s->mf, precision, ctx->jac_precision, kind == GBMHD_PC_MONOLITHIC ? s->reg : nullptr);
   if (rc) return rc;
+  s->factor_gen = ctx->params_gen;
   if (t_setup) *t_setup += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   return 0;
 }
@@ -513,8 +525,8 @@ static int apply_pc(gbmhd_ctx* ctx, int precision, const double* v, double* z, b
   S_CUDA(cudaMemsetAsync(t1 + ctx->offs[1], 0, sizeof(double) * ctx->nfree[1], ctx->stream));
   S_CUDA(cudaMemsetAsync(t1 + ctx->offs[3], 0, sizeof(double) * ctx->nfree[3], ctx->stream));
   double* y = s->w;  // scratch (w is not live during apply_pc in the adjoint path)
-  if ((rc = spmv_t(ctx, s, precision, ctx->offs[1], ctx->offs[2], t1, y))) return rc;
-  if ((rc = spmv_t(ctx, s, precision, ctx->offs[3], n, t1, y))) return rc;
+  if ((rc = spmv_t(ctx, s, ctx->offs[1], ctx->offs[2], t1, y))) return rc;
+  if ((rc = spmv_t(ctx, s, ctx->offs[3], n, t1, y))) return rc;
   // b(p,φ) = v − y
   { k_axpby<<<grid_for(ctx, ctx->nfree[1]), 256, 0, ctx->stream>>>(ctx->nfree[1], -1.0, y + ctx->offs[1], 1.0,
                                                                   b + ctx->offs[1]); gbmhd::count_launch(); }
@@ -536,7 +548,7 @@ static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int
   if (rc) return rc;
   auto op = [&](const double* in, double* out) -> int {
     if (!transpose) return spmv(ctx, precision, in, out);
-    int r = spmv_t(ctx, s, precision, 0, n, in, out);
+    int r = spmv_t(ctx, s, 0, n, in, out);
     return r;
   };
   S_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
@@ -623,7 +635,7 @@ void solver_destroy(gbmhd_ctx* ctx) {
   if (!s) return;
   mf_destroy(s->mf);
   void* ptrs[] = {s->Mp_inv, s->Mf_inv, s->seg, s->V, s->Z, s->w, s->t1, s->t2, s->x32, s->part, s->hdev,
-                  s->rowptrT, s->colT, s->permT};
+                  s->permT, s->valT};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->hhost) cudaFreeHost(s->hhost);
@@ -751,28 +763,31 @@ extern "C" int gbmhd_newton_solve(gbmhd_ctx* ctx, double* x, const gbmhd_solve_o
   return rc;
 }
 
-static int build_transpose(gbmhd_ctx* ctx) {
+// Transposed FP64 Jacobian values for the adjoint (the map once per context, the values
+// after every FP64 assembly).
+static int prepare_transpose(gbmhd_ctx* ctx) {
   Solver* s = ctx->solver;
-  if (s->rowptrT) return 0;
   const int64_t n = ctx->ndofs, nnz = ctx->nnz;
-  std::vector<int64_t> rp(n + 1, 0);
-  for (int64_t t = 0; t < nnz; ++t) rp[ctx->h_col[t] + 1]++;
-  for (int64_t i = 0; i < n; ++i) rp[i + 1] += rp[i];
-  std::vector<int32_t> ct(nnz);
-  std::vector<int64_t> pm(nnz);
-  std::vector<int64_t> fill(rp.begin(), rp.end() - 1);
-  for (int64_t r = 0; r < n; ++r)
-    for (int64_t t = ctx->h_rowptr[r]; t < ctx->h_rowptr[r + 1]; ++t) {
-      const int64_t k = fill[ctx->h_col[t]]++;
-      ct[k] = (int32_t)r;
-      pm[k] = t;
+  if (!s->permT) {
+    int32_t* d_err = nullptr;
+    S_CUDA(cudaMalloc(&s->permT, sizeof(int64_t) * std::max<int64_t>(nnz, 1)));
+    S_CUDA(cudaMalloc(&d_err, sizeof(int32_t)));
+    S_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int32_t), ctx->stream));
+    { k_transpose_map<<<grid_for(ctx, n * 32), 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, s->permT, d_err); gbmhd::count_launch(); }
+    int32_t herr = 0;
+    S_CUDA(cudaMemcpyAsync(&herr, d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    S_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(d_err);
+    if (herr) {
+      cudaFree(s->permT);
+      s->permT = nullptr;
+      ctx->err = "adjoint: the Jacobian pattern is not structurally symmetric";
+      return -3;
     }
-  S_CUDA(cudaMalloc(&s->rowptrT, sizeof(int64_t) * (n + 1)));
-  S_CUDA(cudaMalloc(&s->colT, sizeof(int32_t) * nnz));
-  S_CUDA(cudaMalloc(&s->permT, sizeof(int64_t) * nnz));
-  S_CUDA(cudaMemcpy(s->rowptrT, rp.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
-  S_CUDA(cudaMemcpy(s->colT, ct.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice));
-  S_CUDA(cudaMemcpy(s->permT, pm.data(), sizeof(int64_t) * nnz, cudaMemcpyHostToDevice));
+  }
+  if (!s->valT) S_CUDA(cudaMalloc(&s->valT, sizeof(double) * std::max<int64_t>(nnz, 1)));
+  { k_gather_vals<<<grid_for(ctx, nnz), 256, 0, ctx->stream>>>(nnz, ctx->d_val64, s->permT, s->valT); gbmhd::count_launch(); }
+  S_CUDA(cudaGetLastError());
   return 0;
 }
 
@@ -809,22 +824,21 @@ extern "C" int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x, const gbmhd_object
     ctx->err = "adjoint: copy failed";
     return fail(-2);
   }
-  // Iterative refinement: the outer residual g − Aᵀλ uses the FP64 Jacobian; each correction
-  // solves Aᵀδ = r with FGMRES on the path's operator (FP32 Jacobian in the mixed paths) and
-  // the path's factors.
+  // Iterative refinement on the FP64 transposed Jacobian: each correction solves Aᵀδ = r with
+  // FGMRES (FP64 operator) preconditioned by the path's factors.  The factors of the last
+  // Newton solve on this context are reused when their precision and kind match and the
+  // parameters have not changed since: the refinement converges to the FP64 adjoint
+  // whatever Jacobian they came from.
   const int fprec = o->precision == GBMHD_FP64 ? GBMHD_FP64 : GBMHD_MIXED;
-  const int oprec = fprec;
   if (!ctx->d_val64) {
     if (cudaMalloc(&ctx->d_val64, sizeof(double) * ctx->nnz)) { ctx->err = "adjoint: allocation"; return fail(-2); }
   }
-  if (oprec == GBMHD_MIXED && !ctx->d_val32) {
-    if (cudaMalloc(&ctx->d_val32, sizeof(float) * ctx->nnz)) { ctx->err = "adjoint: allocation"; return fail(-2); }
-  }
   double ta = now_s();
   if ((rc = gb_assemble_device(ctx, d_x, nullptr, 1, GBMHD_FP64))) return fail(rc);
-  if (oprec == GBMHD_MIXED && (rc = gb_assemble_device(ctx, d_x, nullptr, 1, GBMHD_MIXED))) return fail(rc);
-  if ((rc = setup_pc(ctx, fprec, o->preconditioner, &R.time_setup_pc_s))) return fail(rc);
-  if ((rc = build_transpose(ctx))) return fail(rc);
+  const bool reuse = s->mf && mf_precision(s->mf) == fprec && s->pc_kind == o->preconditioner &&
+                     s->factor_gen == ctx->params_gen;
+  if (!reuse && (rc = setup_pc(ctx, fprec, o->preconditioner, &R.time_setup_pc_s))) return fail(rc);
+  if ((rc = prepare_transpose(ctx))) return fail(rc);
   cudaStreamSynchronize(ctx->stream);
   R.time_assembly_s += now_s() - ta;
   double tl = now_s();
@@ -840,23 +854,27 @@ extern "C" int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x, const gbmhd_object
   int total = 0;
   if ((rc = dot(ctx, s, d_g, 1, d_g, &gn))) { cudaFree(d_res); cudaFree(d_del); return fail(rc); }
   gn = std::sqrt(gn);
-  const double inner_rtol = oprec == GBMHD_MIXED ? std::max(o->linear_rtol, 1e-4) : o->linear_rtol;
+  // Each correction solve only has to reduce the current residual to the target; the loop
+  // stops when the true residual no longer halves (the FP64 operator's attainable accuracy).
+  double prev = 1.0;
   for (int k = 0; k < 20 && gn > 0.0; ++k) {
     int iters = 0;
     double irel = 0.0;
-    if ((rc = fgmres(ctx, oprec, d_res, d_del, o->restart, o->max_linear, inner_rtol, true, &iters, &irel,
+    const double inner_rtol = std::min(0.5, std::max(o->linear_rtol / rel, 1e-12));
+    if ((rc = fgmres(ctx, GBMHD_FP64, d_res, d_del, o->restart, o->max_linear, inner_rtol, true, &iters, &irel,
                      o->verbose))) {
       cudaFree(d_res); cudaFree(d_del);
       return fail(rc);
     }
     total += iters;
     { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, d_del, 1.0, d_lam); gbmhd::count_launch(); }
-    if ((rc = spmv_t(ctx, s, GBMHD_FP64, 0, n, d_lam, d_res))) { cudaFree(d_res); cudaFree(d_del); return fail(rc); }
+    if ((rc = spmv_t(ctx, s, 0, n, d_lam, d_res))) { cudaFree(d_res); cudaFree(d_del); return fail(rc); }
     { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, d_g, -1.0, d_res); gbmhd::count_launch(); }
     if ((rc = dot(ctx, s, d_res, 1, d_res, &rn))) { cudaFree(d_res); cudaFree(d_del); return fail(rc); }
     rel = std::sqrt(rn) / gn;
     if (o->verbose) std::fprintf(stderr, "adjoint refinement %d: %d iterations, |g - Aᵀλ|/|g| = %.3e\n", k, iters, rel);
-    if (rel <= o->linear_rtol) break;
+    if (rel <= o->linear_rtol || rel > 0.5 * prev) break;
+    prev = rel;
   }
   cudaFree(d_res);
   cudaFree(d_del);

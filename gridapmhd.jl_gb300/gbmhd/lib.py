@@ -23,7 +23,7 @@ GBMHD_PC_BADIA2024 = 1
 
 SYMBOLS = ["gbmhd_version", "gbmhd_create", "gbmhd_set_params", "gbmhd_sizes", "gbmhd_assemble",
            "gbmhd_assemble_device", "gbmhd_get_csr", "gbmhd_newton_solve", "gbmhd_newton_solve_device",
-           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
+           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_sweep_stats", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -106,6 +106,7 @@ def load(path: Optional[str] = None):
     L.gbmhd_get_stream.argtypes = [C.c_void_p]
     L.gbmhd_get_stream.restype = C.c_void_p
     L.gbmhd_diag_uj_solve_error.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, _dp]
+    L.gbmhd_sweep_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), _dp, _dp]
     L.gbmhd_counters.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.gbmhd_destroy.argtypes = [C.c_void_p]
     L.gbmhd_destroy.restype = None
@@ -233,6 +234,12 @@ class Context:
         self._check(self.L.gbmhd_diag_uj_solve_error(self.h, C.c_void_p(d_state), int(precision), C.byref(e)),
                     "gbmhd_diag_uj_solve_error")
         return e.value
+
+    def sweep_stats(self):
+        """(solves, device seconds, factor bytes per solve) of the multifrontal sweeps since the last call."""
+        a, t, b = C.c_int64(), C.c_double(), C.c_double()
+        self._check(self.L.gbmhd_sweep_stats(self.h, C.byref(a), C.byref(t), C.byref(b)), "gbmhd_sweep_stats")
+        return a.value, t.value, b.value
 
     def stream(self) -> int:
         return int(self.L.gbmhd_get_stream(self.h) or 0)

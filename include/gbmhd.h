@@ -193,6 +193,11 @@ void* gbmhd_get_stream(const gbmhd_ctx* ctx);
  * device state d_state in the given precision. */
 int gbmhd_diag_uj_solve_error(gbmhd_ctx* ctx, const double* d_state, int32_t precision, double* err);
 
+/* Diagnostics: multifrontal solves (preconditioner applications) timed with CUDA events
+ * on the context stream since the last call, their total device time in seconds, and
+ * the factor bytes one solve reads (padding excluded); resets the counters. */
+int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double* bytes_per_apply);
+
 /* Diagnostics: kernels launched by this library and cuBLAS GEMM calls it made
  * since it was loaded (all contexts together). */
 int gbmhd_counters(int64_t* kernel_launches, int64_t* gemm_calls);

@@ -27,8 +27,10 @@ def test_adjoint_matches_oracle(gpu_lib, precision):
     xref, _ = O.newton_direct(prob, np.zeros(dm.ndofs), gauge=[dm.offsets["p"]], rtol=1e-14, maxiter=10)
     dgam, dcw, dfz, _ = oracle_adjoint(prob, dm, xref, g, [dm.offsets["p"]])
     ctx = gpu_context(mesh, dm, params)
+    # the FP64 residual of this case bottoms out near 1e-12 (assembly round-off), so the
+    # absolute stop sits just above it
     x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), precision=precision, max_newton=12, newton_rtol=1e-12,
-                                  newton_atol=1e-13, restart=40, max_linear=400,
+                                  newton_atol=1e-11, restart=40, max_linear=400,
                                   linear_rtol=1e-4 if precision else 1e-8)
     assert rc == 0, rep
     out, lam, arep, arc = ctx.adjoint(x, g, with_cells=True, precision=precision, restart=40, max_linear=400,
@@ -48,9 +50,10 @@ def test_adjoint_matches_gpu_finite_differences(gpu_lib):
     x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), **opts)
     out, lam, arep, arc = ctx.adjoint(x, g, with_cells=False, precision=0, restart=40, max_linear=400,
                                       linear_rtol=1e-11)
-    # FD step 1e-5 (relative): the states come from iterative Newton solves converged to ~1e-13,
-    # whose noise enters the quotient as 1/h; the CPU test checks step 1e-6 with direct solves.
-    h = 1e-5
+    # FD step 1e-4 (relative): the states come from iterative Newton solves converged to
+    # ‖r‖ ~ 1e-14, whose error (~1e-11 in J) enters the quotient as 1/h, while the central
+    # difference's truncation error is O(h²); the CPU test checks step 1e-6 with direct solves.
+    h = 1e-4
     gam = params["gamma"]
     Js = []
     for s in (+1, -1):
