@@ -196,7 +196,7 @@ def run_ours(args):
     n = ctx.ndofs
     stream = torch.cuda.ExternalStream(ctx.stream())
     d_x = torch.zeros(n, dtype=torch.float64, device=dev)
-    opts = dict(precision=lib.GBMHD_MIXED, max_newton=12, newton_rtol=1e-10, restart=200, max_linear=600,
+    opts = dict(precision=lib.GBMHD_MIXED, max_newton=12, newton_rtol=1e-12, restart=200, max_linear=600,
                 linear_rtol=1e-3)
     reps = []
     for _ in range(args.warmup):
@@ -281,7 +281,7 @@ def run_ours(args):
             "data": "synthetic",
             "config": {"workload": "hunt duct 64x64x4, Lz=0.2, tanh(3x) stretching, Ha=500, Re=1, cw=0.1, "
                                    f"zeta={ZETA}", "ncells": mesh.ncells, "ndofs": n, "nnz": ctx.nnz,
-                       "precision": "mixed", "newton_rtol": 1e-10,
+                       "precision": "mixed", "newton_rtol": 1e-12,
                        "l2": "inputs larger than L2 (Jacobian values alone 0.78 GB)"},
             "newton_solve_s": ms / 1e3, "newton_iters": last["newton_iters"], "linear_iters": last["linear_iters"],
             "time_split_s": {k: last[k] for k in ("time_assembly_s", "time_setup_pc_s", "time_linear_s")},

@@ -1,5 +1,6 @@
 // Numeric multifrontal factorization and solves of the (u,j) block (see mf.h).
 #include <cublas_v2.h>
+#include <cuda.h>  // CUtensorMap types; the encoder is reached through the runtime's driver entry point
 
 #include <cstdlib>
 #include <cstring>
@@ -51,6 +52,12 @@ struct MFNumeric {
   int64_t tsave_len = 0;
   int32_t* d_err = nullptr;    // device-side status (singular pivot block)
   int fp32_gemm_mode = 0;      // 0: BF16x9 emulated FP32, 1: plain FP32
+  // TMA-staged sweeps (FP32 factors): one 3-D tensor map per level (rows x columns x fronts)
+  std::vector<CUtensorMap> maps;
+  std::vector<char> map_ok;
+  const void* maps_base = nullptr;
+  int32_t* d_sweep_err = nullptr;   // set by a sweep whose TMA wait timed out
+  int32_t* h_sweep_err = nullptr;   // pinned copy, read at the next solve
   // sweep timing: events around each solve, harvested when the next one starts
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ev_pending = false;
@@ -151,6 +158,10 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
     const int64_t ne = S.f_ne[f], nb = S.f_nb[f];
     M->sweep_elems += nb * ne + ne * (ne + nb);
   }
+  MF_CUDA(cudaMalloc(&M->d_sweep_err, sizeof(int32_t)));
+  MF_CUDA(cudaMemset(M->d_sweep_err, 0, sizeof(int32_t)));
+  MF_CUDA(cudaMallocHost(&M->h_sweep_err, sizeof(int32_t)));
+  *M->h_sweep_err = 0;
   MF_CUDA(cudaEventCreate(&M->ev0));
   MF_CUDA(cudaEventCreate(&M->ev1));
   if ((rc = upload(ctx, &M->tsave_off, toff))) return rc;
@@ -163,6 +174,10 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
     return -2;
   }
   MF_BLAS(cublasSetStream(M->blas, ctx->stream));
+  // Front entries are finite (a singular pivot block raises the factorization error and a
+  // non-finite FGMRES residual ends the solve), so the BF16x9 emulation need not scan its
+  // operands for infinities and NaNs before every GEMM.
+  MF_BLAS(cublasSetEmulationSpecialValuesSupport(M->blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE));
   const char* mode = std::getenv("GBMHD_FP32_GEMM");
   M->fp32_gemm_mode = (mode && std::strcmp(mode, "fp32") == 0) ? 1 : 0;
   return 0;
@@ -176,6 +191,8 @@ void mf_destroy(MFNumeric* M) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (M->blas) cublasDestroy(M->blas);
+  if (M->d_sweep_err) cudaFree(M->d_sweep_err);
+  if (M->h_sweep_err) cudaFreeHost(M->h_sweep_err);
   if (M->ev0) cudaEventDestroy(M->ev0);
   if (M->ev1) cudaEventDestroy(M->ev1);
   delete M;
@@ -314,10 +331,25 @@ __global__ void __launch_bounds__(256) k_pivot_inverse(const T* __restrict__ F, 
 // pipes (~48 significant bits; the result is rounded to FP32).  GB300 issues FP64 at a
 // small fraction of its FP32 rate: the kb³ updates cost ~14 FP32 operations each here
 // instead of one FP64 FMA, which is still several times faster.  The per-column scalars
-// (the pivot's reciprocal, the scaled pivot row) are formed in FP64.
-__device__ __forceinline__ void df_split(double x, float& h, float& l) {
-  h = (float)x;
-  l = (float)(x - (double)h);
+// (the pivot's reciprocal, the scaled pivot row) are float-float too; the pivot is chosen on
+// the high parts.
+// float-float product (Dekker via FMA) and reciprocal (one Newton step on the FP32 one)
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& h, float& l) {
+  const float p = __fmul_rn(ah, bh);
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  h = __fadd_rn(p, e);
+  l = __fsub_rn(e, __fsub_rn(h, p));
+}
+
+__device__ __forceinline__ void df_rcp(float ah, float al, float& h, float& l) {
+  const float x = __frcp_rn(ah);
+  float e = fmaf(-ah, x, 1.0f);  // 1 − ah·x, exact
+  e = fmaf(-al, x, e);
+  const float d = __fmul_rn(x, e);
+  h = __fadd_rn(x, d);
+  l = __fsub_rn(d, __fsub_rn(h, x));
 }
 
 __global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restrict__ F, int64_t off, int n, int k,
@@ -338,22 +370,22 @@ __global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restric
     }
   __syncthreads();
   for (int c = 0; c < kb; ++c) {
-    if (tid < 32) {  // argmax |A[i, c]| over rows c..kb-1 (ties: the lower row)
-      double best = -1.0;
+    if (tid < 32) {  // argmax |A[i, c]| (high parts) over rows c..kb-1 (ties: the lower row)
+      float best = -1.0f;
       int bi = c;
       for (int i = c + tid; i < kb; i += 32) {
-        const double a = fabs((double)Ah[i + c * kb] + (double)Al[i + c * kb]);
+        const float a = fabsf(Ah[i + c * kb]);
         if (a > best) { best = a; bi = i; }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const float ob = __shfl_down_sync(0xffffffffu, best, o);
         const int oi = __shfl_down_sync(0xffffffffu, bi, o);
         if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
       }
       if (tid == 0) {
         piv_row = bi;
         perm[c] = bi;
-        if (!(best > 0.0)) atomicExch(err, 1);
+        if (!(best > 0.0f)) atomicExch(err, 1);
       }
     }
     __syncthreads();
@@ -368,10 +400,11 @@ __global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restric
     }
     __syncthreads();
     if (tid < kb) {
-      const double d = (double)Ah[c + c * kb] + (double)Al[c + c * kb];
-      const double inv = d != 0.0 ? 1.0 / d : 0.0;
-      const double r = tid == c ? inv : ((double)Ah[c + tid * kb] + (double)Al[c + tid * kb]) * inv;
-      df_split(r, rh[tid], rl[tid]);
+      float ih = 0.0f, il = 0.0f;  // 1 / A[c, c] in float-float
+      const float dh = Ah[c + c * kb], dl = Al[c + c * kb];
+      if (dh != 0.0f) df_rcp(dh, dl, ih, il);
+      if (tid == c) { rh[tid] = ih; rl[tid] = il; }
+      else df_mul(Ah[c + tid * kb], Al[c + tid * kb], ih, il, rh[tid], rl[tid]);
       if (tid == c) { mh[tid] = 0.0f; ml[tid] = 0.0f; }
       else { mh[tid] = Ah[tid + c * kb]; ml[tid] = Al[tid + c * kb]; }
     }
@@ -697,6 +730,147 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_chunk(const T* __restrict__ 
     if (i0 + r < ne) atomicAdd(&ybuf[toff[f] + i0 + r], acc[r].value());
 }
 
+// ---- TMA-staged sweeps (FP32 factors)
+// A CTA owns a tile of TS_ROWS rows of one front and a chunk of its columns.  Thread 0
+// streams the chunk through shared memory in stages of TS_COLS columns with
+// cp.async.bulk.tensor (one 3-D tensor map per level: rows x columns x fronts), keeping
+// TS_STAGES stages in flight behind mbarriers; every thread reduces two rows of each staged
+// column in float-float arithmetic.  The forward sweep reads the boundary rows of the
+// eliminated columns, the backward sweep the eliminated rows of the eliminated columns
+// and of the boundary columns (two column segments, chunked separately).
+constexpr int TS_ROWS = 256;
+constexpr int TS_COLS = 16;
+constexpr int TS_STAGES = 4;
+constexpr int TS_THREADS = TS_ROWS / 2;
+constexpr long TS_WAIT_LIMIT = 1L << 22;  // bounded mbarrier waits
+constexpr size_t TS_TILE_BYTES = (size_t)TS_STAGES * TS_COLS * TS_ROWS * sizeof(float);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase) {
+  for (long i = 0; i < TS_WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// FWD: b[bnd_j] += Σ_{c<ne} M[E+j, c] t_c.   BWD: ybuf_i += Σ_v M[i, col(v)] w_v over v in this
+// CTA's chunk, w = [t ; −x_B], col(v) = v (v < ne) or E + (v − ne).
+template <bool FWD>
+__global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant__ CUtensorMap map, int64_t first,
+                                                          int E, int cw, int chunks_a, double* __restrict__ b,
+                                                          const double* __restrict__ x,
+                                                          const double* __restrict__ tsave,
+                                                          const int64_t* __restrict__ toff,
+                                                          const int32_t* __restrict__ bnd,
+                                                          const int64_t* __restrict__ bnd_ptr,
+                                                          const int32_t* __restrict__ f_ne,
+                                                          const int32_t* __restrict__ f_nb, double* __restrict__ ybuf,
+                                                          int32_t* err) {
+  extern __shared__ __align__(1024) unsigned char ts_raw[];
+  float* tiles = reinterpret_cast<float*>(ts_raw);                  // [stage][column][row]
+  float2* vs = reinterpret_cast<float2*>(ts_raw + TS_TILE_BYTES);   // [cw] vector segment, float-float
+  __shared__ __align__(8) uint64_t full[TS_STAGES];
+  __shared__ int abort_flag;
+  const int fl = blockIdx.z;
+  const int64_t f = first + fl;
+  const int ne = f_ne[f], nb = f_nb[f];
+  const int nrows = FWD ? nb : ne;
+  const int row0 = blockIdx.x * TS_ROWS;
+  if (row0 >= nrows) return;
+  const bool seg_b = !FWD && (int)blockIdx.y >= chunks_a;
+  const int c0 = (seg_b ? (int)blockIdx.y - chunks_a : (int)blockIdx.y) * cw;
+  const int c1 = min(seg_b ? nb : ne, c0 + cw);
+  if (c0 >= c1) return;
+  const int ncol = c1 - c0;
+  const int pcol0 = seg_b ? E + c0 : c0;
+  const int prow0 = (FWD ? E : 0) + row0;
+  const int nst = (ncol + TS_COLS - 1) / TS_COLS;
+  constexpr uint32_t stage_bytes = TS_COLS * TS_ROWS * sizeof(float);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TS_STAGES; ++s) mbar_init(&full[s], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int s = 0; s < min(TS_STAGES, nst); ++s) {
+      mbar_expect_tx(&full[s], stage_bytes);
+      tma_load_3d(tiles + (size_t)s * TS_COLS * TS_ROWS, &map, prow0, pcol0 + s * TS_COLS, fl, &full[s]);
+    }
+  const double* t = tsave + toff[f];
+  const int32_t* bd = bnd + bnd_ptr[f];
+  for (int c = threadIdx.x; c < ncol; c += blockDim.x)
+    vs[c] = SweepAcc<float>::pack(seg_b ? -x[bd[c0 + c]] : t[c0 + c]);
+  __syncthreads();
+  SweepAcc<float> a0, a1;
+  const int r = 2 * threadIdx.x;
+  for (int s = 0; s < nst; ++s) {
+    const int buf = s % TS_STAGES;
+    if (mbar_wait_bounded(&full[buf], (uint32_t)(s / TS_STAGES) & 1u)) {
+      const float* tile = tiles + (size_t)buf * TS_COLS * TS_ROWS;
+      const float2* vv = vs + s * TS_COLS;
+      const int cn = min(TS_COLS, ncol - s * TS_COLS);
+#pragma unroll 4
+      for (int c = 0; c < cn; ++c) {
+        const float2 m = *reinterpret_cast<const float2*>(tile + c * TS_ROWS + r);
+        const float2 v = vv[c];
+        a0.add(m.x, v);
+        a1.add(m.y, v);
+      }
+    } else {
+      abort_flag = 1;
+    }
+    __syncthreads();
+    if (abort_flag) {
+      if (threadIdx.x == 0) {  // let the copies in flight land before the CTA's shared memory is released
+        for (int s2 = s; s2 < min(nst, s + TS_STAGES); ++s2)
+          mbar_wait_bounded(&full[s2 % TS_STAGES], (uint32_t)(s2 / TS_STAGES) & 1u);
+        atomicExch(err, 1);
+      }
+      return;
+    }
+    if (threadIdx.x == 0 && s + TS_STAGES < nst) {
+      mbar_expect_tx(&full[buf], stage_bytes);
+      tma_load_3d(tiles + (size_t)buf * TS_COLS * TS_ROWS, &map, prow0, pcol0 + (s + TS_STAGES) * TS_COLS, fl,
+                  &full[buf]);
+    }
+  }
+  const int i0 = row0 + r;
+  if (FWD) {
+    if (i0 < nb) atomicAdd(&b[bd[i0]], a0.value());
+    if (i0 + 1 < nb) atomicAdd(&b[bd[i0 + 1]], a1.value());
+  } else {
+    double* y = ybuf + toff[f];
+    if (i0 < ne) atomicAdd(&y[i0], a0.value());
+    if (i0 + 1 < ne) atomicAdd(&y[i0 + 1], a1.value());
+  }
+}
+
 __global__ void k_bwd_scatter(double* __restrict__ x, double* __restrict__ ybuf, const int64_t* __restrict__ toff,
                               const int32_t* __restrict__ elim, const int64_t* __restrict__ elim_ptr,
                               const int32_t* __restrict__ f_ne, int64_t first) {
@@ -711,6 +885,60 @@ __global__ void k_bwd_scatter(double* __restrict__ x, double* __restrict__ ybuf,
 }
 
 // ------------------------------------------------------------------ host drivers
+// ---- tensor maps of the TMA-staged sweeps
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// One map per level over the FP32 fronts: dims (n rows, n columns, count fronts), box
+// (TS_ROWS, TS_COLS, 1).  A level whose fronts are narrower than a box keeps the LDG sweeps.
+static void build_sweep_maps(MFNumeric* M) {
+  const MFSymbolic& S = M->S;
+  M->maps.assign(S.levels.size(), CUtensorMap{});
+  M->map_ok.assign(S.levels.size(), 0);
+  M->maps_base = M->F;
+  EncodeTiledFn enc = encode_tiled_fn();
+  if (!enc) return;
+  float* F = reinterpret_cast<float*>(M->F);
+  for (size_t l = 0; l < S.levels.size(); ++l) {
+    const MFLevel& L = S.levels[l];
+    if (L.n < TS_ROWS || L.count > (1 << 16)) continue;
+    const cuuint64_t dims[3] = {(cuuint64_t)L.n, (cuuint64_t)L.n, (cuuint64_t)L.count};
+    const cuuint64_t strides[2] = {(cuuint64_t)L.n * sizeof(float), (cuuint64_t)L.n * L.n * sizeof(float)};
+    const cuuint32_t box[3] = {TS_ROWS, TS_COLS, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    if (enc(&M->maps[l], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, F + L.off, dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+      M->map_ok[l] = 1;
+  }
+}
+
+// Column chunk of the TMA sweeps: a multiple of TS_COLS, about two waves of three resident
+// CTAs per SM for the level.
+static int tma_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t fronts) {
+  const int64_t per_chunk = std::max<int64_t>(1, (rows + TS_ROWS - 1) / TS_ROWS) * std::max<int64_t>(1, fronts);
+  const int64_t want = (int64_t)ctx->num_sms * 6;
+  const int64_t chunks = std::max<int64_t>(1, (want + per_chunk - 1) / per_chunk);
+  int64_t cols = (ncols + chunks - 1) / chunks;
+  cols = ((cols + TS_COLS - 1) / TS_COLS) * TS_COLS;
+  return (int)std::max<int64_t>(TS_COLS, std::min<int64_t>(cols, 1024));
+}
+
 template <typename T>
 static cublasStatus_t gemm_sb(MFNumeric* M, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
                               const T* alpha, const T* A, int lda, long long sA, const T* B, int ldb, long long sB,
@@ -834,6 +1062,7 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
     return -3;
   }
   M->precision = sizeof(T) == 8 ? GBMHD_FP64 : GBMHD_MIXED;
+  if (sizeof(T) == 4 && M->maps_base != M->F) build_sweep_maps(M);
   return 0;
 }
 
@@ -871,7 +1100,13 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     const int cnt = (int)L.count;
     { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first, L.E); gbmhd::count_launch(); }
     if (L.B > 0) {
-      if (!tr) {
+      if (!tr && sizeof(T) == 4 && M->map_ok[l]) {
+        const int cw = tma_cols(ctx, L.B, L.E, cnt);
+        dim3 g((unsigned)((L.B + TS_ROWS - 1) / TS_ROWS), (unsigned)((L.E + cw - 1) / cw), (unsigned)cnt);
+        const size_t sm = TS_TILE_BYTES + sizeof(float2) * cw;
+        MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        { k_sweep_tma<true><<<g, TS_THREADS, sm, ctx->stream>>>(M->maps[l], L.first, L.E, cw, 0, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, M->d_sweep_err); gbmhd::count_launch(); }
+      } else if (!tr) {
         const int cols = sweep_cols(ctx, L.B, L.E, cnt, rows_cta);
         dim3 g((unsigned)((L.B + rows_cta - 1) / rows_cta), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
         { k_fwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
@@ -888,7 +1123,15 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
   for (int l = (int)S.levels.size() - 1; l >= 0; --l) {
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count;
-    if (!tr) {
+    if (!tr && sizeof(T) == 4 && M->map_ok[l]) {
+      const int cw = tma_cols(ctx, L.E, L.n, cnt);
+      const int ca = (L.E + cw - 1) / cw, cb = (L.B + cw - 1) / cw;
+      dim3 g((unsigned)((L.E + TS_ROWS - 1) / TS_ROWS), (unsigned)(ca + cb), (unsigned)cnt);
+      const size_t sm = TS_TILE_BYTES + sizeof(float2) * cw;
+      MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      { k_sweep_tma<false><<<g, TS_THREADS, sm, ctx->stream>>>(M->maps[l], L.first, L.E, cw, ca, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, M->d_sweep_err); gbmhd::count_launch(); }
+      { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
+    } else if (!tr) {
       const int cols = sweep_cols(ctx, L.E, L.n, cnt, rows_cta);
       dim3 g((unsigned)((L.E + rows_cta - 1) / rows_cta), (unsigned)((L.n + cols - 1) / cols), (unsigned)cnt);
       { k_bwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
@@ -910,6 +1153,10 @@ int mf_solve(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transp
     ctx->err = "multifrontal: not factored";
     return -1;
   }
+  if (*M->h_sweep_err) {  // set by an earlier solve whose copies arrived; this one cannot be trusted
+    ctx->err = "multifrontal: a solve sweep's TMA wait timed out";
+    return -3;
+  }
   harvest_sweep_time(M, false);
   const bool timed = !M->ev_pending && M->ev0 && M->ev1;
   if (timed) MF_CUDA(cudaEventRecord(M->ev0, ctx->stream));
@@ -920,5 +1167,6 @@ int mf_solve(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transp
     MF_CUDA(cudaEventRecord(M->ev1, ctx->stream));
     M->ev_pending = true;
   }
+  MF_CUDA(cudaMemcpyAsync(M->h_sweep_err, M->d_sweep_err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
   return 0;
 }
