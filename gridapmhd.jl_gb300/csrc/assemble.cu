@@ -39,6 +39,11 @@ struct CellWork {
   int32_t row[ND];
   unsigned long long sign;
   int32_t pad;
+  T wdT[NQ];            // w det J in the element-matrix precision
+  T idetT[NQ];
+  T JinvT[NQ][9];
+  T JdT[NQ][9];
+  T valT[ND];           // local state in the element-matrix precision
   T G[NQ][3][27];       // physical Q2 gradients  [q][i][n]
   T S[NQ][3][36];       // physical RT values     [q][i][b]
   T Sdiv[NQ][36];
@@ -103,6 +108,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
     if (tid < 24) w.X[tid] = A.cellX[cell * 24 + tid];
     for (int a = tid; a < ND; a += nth) {  // ND = 129 slots: more than one pass for 128 threads
       w.val[a] = A.xfull[A.gidx[cell * ND + a]];
+      w.valT[a] = (T)w.val[a];
       const int32_t rr = A.row[cell * ND + a];
       w.row[a] = rr;
       w.rbase[a] = rr >= 0 ? A.rowptr[rr] : -1;
@@ -134,27 +140,37 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
       Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
       Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
       w.wdet[q] = geo.w[q] * det;
+      // FP64 geometry, rounded once to the element-matrix precision: FP64 converts and FMAs in
+      // the per-entry loops bound this kernel on GB300's FP64 issue rate
+      w.wdT[q] = (T)w.wdet[q];
       w.idet[q] = id;
+      w.idetT[q] = (T)id;
       for (int e = 0; e < 3; ++e)
-        for (int i = 0; i < 3; ++i) w.Jinv[q][e * 3 + i] = Ji[e][i];
+        for (int i = 0; i < 3; ++i) {
+          w.Jinv[q][e * 3 + i] = Ji[e][i];
+          w.JinvT[q][e * 3 + i] = (T)Ji[e][i];
+        }
       for (int i = 0; i < 3; ++i)
-        for (int m = 0; m < 3; ++m) w.Jd[q][i * 3 + m] = J[i][m] * id;
+        for (int m = 0; m < 3; ++m) {
+          w.Jd[q][i * 3 + m] = J[i][m] * id;
+          w.JdT[q][i * 3 + m] = (T)(J[i][m] * id);
+        }
     }
     __syncthreads();
     // ---------------------------------------------------------------- physical bases
     for (int idx = tid; idx < NQ * 27; idx += nth) {
       const int q = idx / 27, n = idx % 27;
-      const double g0 = (double)tb.g2[q][n][0], g1 = (double)tb.g2[q][n][1], g2 = (double)tb.g2[q][n][2];
+      const T g0 = tb.g2[q][n][0], g1 = tb.g2[q][n][1], g2 = tb.g2[q][n][2];
       for (int i = 0; i < 3; ++i)
-        w.G[q][i][n] = (T)(w.Jinv[q][0 * 3 + i] * g0 + w.Jinv[q][1 * 3 + i] * g1 + w.Jinv[q][2 * 3 + i] * g2);
+        w.G[q][i][n] = w.JinvT[q][0 * 3 + i] * g0 + w.JinvT[q][1 * 3 + i] * g1 + w.JinvT[q][2 * 3 + i] * g2;
     }
     for (int idx = tid; idx < NQ * 36; idx += nth) {
       const int q = idx / 36, b = idx % 36;
       const int d = b / 12;
-      const double sg = ((w.sign >> b) & 1ull) ? -1.0 : 1.0;
-      const double r = (double)tb.rt[q][b] * sg;
-      for (int i = 0; i < 3; ++i) w.S[q][i][b] = (T)(w.Jd[q][i * 3 + d] * r);
-      w.Sdiv[q][b] = (T)((double)tb.rtdiv[q][b] * sg * w.idet[q]);
+      const T sg = ((w.sign >> b) & 1ull) ? (T)-1 : (T)1;
+      const T r = tb.rt[q][b] * sg;
+      for (int i = 0; i < 3; ++i) w.S[q][i][b] = w.JdT[q][i * 3 + d] * r;
+      w.Sdiv[q][b] = tb.rtdiv[q][b] * sg * w.idetT[q];
     }
     __syncthreads();
     // ---------------------------------------------------------------- state at the points
@@ -163,7 +179,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
         const int q = idx / 3, c = idx % 3;
         T uc = 0, g0 = 0, g1 = 0, g2 = 0;
         for (int n = 0; n < 27; ++n) {
-          const T v = (T)w.val[OU + c * 27 + n];
+          const T v = w.valT[OU + c * 27 + n];
           uc += v * tb.n2[q][n];
           g0 += v * w.G[q][0][n];
           g1 += v * w.G[q][1][n];
@@ -177,17 +193,17 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
         const int k = idx - NQ * 3;
         const int q = k / 3, i = k % 3;
         T s = 0;
-        for (int b = 0; b < 36; ++b) s += (T)w.val[OJ + b] * w.S[q][i][b];
+        for (int b = 0; b < 36; ++b) s += w.valT[OJ + b] * w.S[q][i][b];
         w.jv[q][i] = s;
         if (i == 0) {
           T dv = 0;
-          for (int b = 0; b < 36; ++b) dv += (T)w.val[OJ + b] * w.Sdiv[q][b];
+          for (int b = 0; b < 36; ++b) dv += w.valT[OJ + b] * w.Sdiv[q][b];
           w.divj[q] = dv;
           T p = 0;
-          for (int m = 0; m < 4; ++m) p += (T)w.val[OP + m] * tb.p1[q][m];
+          for (int m = 0; m < 4; ++m) p += w.valT[OP + m] * tb.p1[q][m];
           w.pp[q] = p;
           T f = 0;
-          for (int m = 0; m < 8; ++m) f += (T)w.val[OPHI + m] * tb.q1[q][m];
+          for (int m = 0; m < 8; ++m) f += w.valT[OPHI + m] * tb.q1[q][m];
           w.ph[q] = f;
         }
       }
@@ -199,7 +215,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
       for (int idx = tid; idx < 4 * 81; idx += nth) {
         const int k = idx / 81, ca = idx % 81, c = ca / 27, a = ca % 27;
         T s = 0;
-        for (int q = 0; q < NQ; ++q) s += (T)w.wdet[q] * tb.p1[q][k] * w.G[q][c][a];
+        for (int q = 0; q < NQ; ++q) s += w.wdT[q] * tb.p1[q][k] * w.G[q][c][a];
         w.Bd[k][ca] = s;
       }
       if (tid == 0) {
@@ -309,7 +325,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
     const bool conv = P.convection != 0, newton = P.convection == 2;
     for (int idx = tid; idx < NQ * 27; idx += nth) {
       const int q = idx / 27, b = idx % 27;
-      w.ugb[q][b] = (T)w.wdet[q] * (w.u[q][0] * w.G[q][0][b] + w.u[q][1] * w.G[q][1][b] + w.u[q][2] * w.G[q][2][b]);
+      w.ugb[q][b] = w.wdT[q] * (w.u[q][0] * w.G[q][0][b] + w.u[q][1] * w.G[q][1][b] + w.u[q][2] * w.G[q][2][b]);
     }
     __syncthreads();
     const T beta = (T)P.beta, alpha = (T)P.alpha, gam = (T)P.gamma, sig = (T)P.sigma;
@@ -321,7 +337,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
       const int a = idx / 27, b = idx % 27;
       T K = 0, Cv = 0;
       for (int q = 0; q < NQ; ++q) {
-        const T wd = (T)w.wdet[q];
+        const T wd = w.wdT[q];
         K += wd * (w.G[q][0][a] * w.G[q][0][b] + w.G[q][1][a] * w.G[q][1][b] + w.G[q][2][a] * w.G[q][2][b]);
         if (conv) Cv += tb.n2[q][a] * w.ugb[q][b];
       }
@@ -330,7 +346,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
         T M0 = 0, M1 = 0, M2 = 0;
         if (newton) {
           for (int q = 0; q < NQ; ++q) {
-            const T m = (T)w.wdet[q] * tb.n2[q][a] * tb.n2[q][b];
+            const T m = w.wdT[q] * tb.n2[q][a] * tb.n2[q][b];
             M0 += m * w.gu[q][0 * 3 + c];
             M1 += m * w.gu[q][1 * 3 + c];
             M2 += m * w.gu[q][2 * 3 + c];
@@ -357,7 +373,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
     for (int idx = tid; idx < 81 * 4; idx += nth) {
       const int ca = idx / 4, k = idx % 4, c = ca / 27, a = ca % 27;
       T s = 0;
-      for (int q = 0; q < NQ; ++q) s += (T)w.wdet[q] * tb.p1[q][k] * w.G[q][c][a];
+      for (int q = 0; q < NQ; ++q) s += w.wdT[q] * tb.p1[q][k] * w.G[q][c][a];
       const int ru = OU + ca, rp = OP + k;
       if (w.row[ru] >= 0) {
         red_add(&val[w.rbase[ru] + ot[ru * ND + rp]], -s);
@@ -369,7 +385,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
       const int a = idx / 36, b = idx % 36;
       T c0 = 0, c1 = 0, c2 = 0;
       for (int q = 0; q < NQ; ++q) {
-        const T m = (T)w.wdet[q] * tb.n2[q][a];
+        const T m = w.wdT[q] * tb.n2[q][a];
         const T s0 = w.S[q][0][b], s1 = w.S[q][1][b], s2 = w.S[q][2][b];
         c0 += m * (s1 * B2 - s2 * B1);
         c1 += m * (s2 * B0 - s0 * B2);
@@ -394,7 +410,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
       for (int q = 0; q < NQ; ++q) {
         T t = w.S[q][0][a] * w.S[q][0][b] + w.S[q][1][a] * w.S[q][1][b] + w.S[q][2][a] * w.S[q][2][b];
         if (P.zeta_j != 0.0) t += zj * w.Sdiv[q][a] * w.Sdiv[q][b];
-        s += (T)w.wdet[q] * t;
+        s += w.wdT[q] * t;
       }
       red_add(&val[w.rbase[ra] + ot[ra * ND + rb]], s);
     }
@@ -404,7 +420,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
       const int rj = OJ + b, rf = OPHI + k;
       if (w.row[rj] < 0) continue;
       T s = 0;
-      for (int q = 0; q < NQ; ++q) s += (T)w.wdet[q] * tb.q1[q][k] * w.Sdiv[q][b];
+      for (int q = 0; q < NQ; ++q) s += w.wdT[q] * tb.q1[q][k] * w.Sdiv[q][b];
       red_add(&val[w.rbase[rj] + ot[rj * ND + rf]], -sig * s);
       red_add(&val[w.rbase[rf] + ot[rf * ND + rj]], -s);
     }

@@ -54,6 +54,7 @@ struct MFNumeric {
   int fp32_gemm_mode = 0;      // 0: BF16x9 emulated FP32, 1: plain FP32
   // TMA-staged sweeps (FP32 factors): one 3-D tensor map per level (rows x columns x fronts)
   std::vector<CUtensorMap> maps;
+  std::vector<int> map_rows;      // row tile of each map
   std::vector<char> map_ok;
   const void* maps_base = nullptr;
   int32_t* d_sweep_err = nullptr;   // set by a sweep whose TMA wait timed out
@@ -731,7 +732,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_chunk(const T* __restrict__ 
 }
 
 // ---- TMA-staged sweeps (FP32 factors)
-// A CTA owns a tile of TS_ROWS rows of one front and a chunk of its columns.  Thread 0
+// A CTA owns a tile of `rows` rows (at most TS_ROWS, sized per level so that the tiles cover
+// the level's rows with little overhang) of one front and a chunk of its columns.  Thread 0
 // streams the chunk through shared memory in stages of TS_COLS columns with
 // cp.async.bulk.tensor (one 3-D tensor map per level: rows x columns x fronts), keeping
 // TS_STAGES stages in flight behind mbarriers; every thread reduces two rows of each staged
@@ -741,9 +743,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_bwd_chunk(const T* __restrict__ 
 constexpr int TS_ROWS = 256;
 constexpr int TS_COLS = 16;
 constexpr int TS_STAGES = 4;
-constexpr int TS_THREADS = TS_ROWS / 2;
+constexpr int TS_THREADS = TS_ROWS / 2;   // launch bound; a level uses rows / 2 threads
 constexpr long TS_WAIT_LIMIT = 1L << 22;  // bounded mbarrier waits
-constexpr size_t TS_TILE_BYTES = (size_t)TS_STAGES * TS_COLS * TS_ROWS * sizeof(float);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -782,7 +783,8 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 // CTA's chunk, w = [t ; −x_B], col(v) = v (v < ne) or E + (v − ne).
 template <bool FWD>
 __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant__ CUtensorMap map, int64_t first,
-                                                          int E, int cw, int chunks_a, double* __restrict__ b,
+                                                          int E, int rows, int cw, int chunks_a,
+                                                          double* __restrict__ b,
                                                           const double* __restrict__ x,
                                                           const double* __restrict__ tsave,
                                                           const int64_t* __restrict__ toff,
@@ -793,14 +795,14 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
                                                           int32_t* err) {
   extern __shared__ __align__(1024) unsigned char ts_raw[];
   float* tiles = reinterpret_cast<float*>(ts_raw);                  // [stage][column][row]
-  float2* vs = reinterpret_cast<float2*>(ts_raw + TS_TILE_BYTES);   // [cw] vector segment, float-float
+  float2* vs = reinterpret_cast<float2*>(ts_raw + (size_t)TS_STAGES * TS_COLS * rows * sizeof(float));  // [cw]
   __shared__ __align__(8) uint64_t full[TS_STAGES];
   __shared__ int abort_flag;
   const int fl = blockIdx.z;
   const int64_t f = first + fl;
   const int ne = f_ne[f], nb = f_nb[f];
   const int nrows = FWD ? nb : ne;
-  const int row0 = blockIdx.x * TS_ROWS;
+  const int row0 = blockIdx.x * rows;
   if (row0 >= nrows) return;
   const bool seg_b = !FWD && (int)blockIdx.y >= chunks_a;
   const int c0 = (seg_b ? (int)blockIdx.y - chunks_a : (int)blockIdx.y) * cw;
@@ -810,7 +812,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
   const int pcol0 = seg_b ? E + c0 : c0;
   const int prow0 = (FWD ? E : 0) + row0;
   const int nst = (ncol + TS_COLS - 1) / TS_COLS;
-  constexpr uint32_t stage_bytes = TS_COLS * TS_ROWS * sizeof(float);
+  const uint32_t stage_bytes = TS_COLS * rows * sizeof(float);
   if (threadIdx.x == 0) {
     for (int s = 0; s < TS_STAGES; ++s) mbar_init(&full[s], 1);
     abort_flag = 0;
@@ -820,7 +822,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
   if (threadIdx.x == 0)
     for (int s = 0; s < min(TS_STAGES, nst); ++s) {
       mbar_expect_tx(&full[s], stage_bytes);
-      tma_load_3d(tiles + (size_t)s * TS_COLS * TS_ROWS, &map, prow0, pcol0 + s * TS_COLS, fl, &full[s]);
+      tma_load_3d(tiles + (size_t)s * TS_COLS * rows, &map, prow0, pcol0 + s * TS_COLS, fl, &full[s]);
     }
   const double* t = tsave + toff[f];
   const int32_t* bd = bnd + bnd_ptr[f];
@@ -832,12 +834,12 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
   for (int s = 0; s < nst; ++s) {
     const int buf = s % TS_STAGES;
     if (mbar_wait_bounded(&full[buf], (uint32_t)(s / TS_STAGES) & 1u)) {
-      const float* tile = tiles + (size_t)buf * TS_COLS * TS_ROWS;
+      const float* tile = tiles + (size_t)buf * TS_COLS * rows;
       const float2* vv = vs + s * TS_COLS;
       const int cn = min(TS_COLS, ncol - s * TS_COLS);
 #pragma unroll 4
       for (int c = 0; c < cn; ++c) {
-        const float2 m = *reinterpret_cast<const float2*>(tile + c * TS_ROWS + r);
+        const float2 m = *reinterpret_cast<const float2*>(tile + c * rows + r);
         const float2 v = vv[c];
         a0.add(m.x, v);
         a1.add(m.y, v);
@@ -856,7 +858,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
     }
     if (threadIdx.x == 0 && s + TS_STAGES < nst) {
       mbar_expect_tx(&full[buf], stage_bytes);
-      tma_load_3d(tiles + (size_t)buf * TS_COLS * TS_ROWS, &map, prow0, pcol0 + (s + TS_STAGES) * TS_COLS, fl,
+      tma_load_3d(tiles + (size_t)buf * TS_COLS * rows, &map, prow0, pcol0 + (s + TS_STAGES) * TS_COLS, fl,
                   &full[buf]);
     }
   }
@@ -904,34 +906,50 @@ static EncodeTiledFn encode_tiled_fn() {
   return fn;
 }
 
-// One map per level over the FP32 fronts: dims (n rows, n columns, count fronts), box
-// (TS_ROWS, TS_COLS, 1).  A level whose fronts are narrower than a box keeps the LDG sweeps.
+// Row tile of a sweep over `nrows` rows: the fewest tiles of at most TS_ROWS rows, each a
+// multiple of 32 rows (16 threads), so that the TMA boxes overhang the rows little.
+static int tma_rows(int nrows) {
+  const int tiles = std::max(1, (nrows + TS_ROWS - 1) / TS_ROWS);
+  const int per = (nrows + tiles - 1) / tiles;
+  return std::min(TS_ROWS, std::max(32, (per + 31) / 32 * 32));
+}
+
+// Two maps per level over the FP32 fronts (forward: boundary rows, backward: eliminated
+// rows): dims (n rows, n columns, count fronts), box (rows, TS_COLS, 1).  A level whose
+// fronts are narrower than a box keeps the LDG sweeps.
 static void build_sweep_maps(MFNumeric* M) {
   const MFSymbolic& S = M->S;
-  M->maps.assign(S.levels.size(), CUtensorMap{});
-  M->map_ok.assign(S.levels.size(), 0);
+  const size_t nl = S.levels.size();
+  M->maps.assign(2 * nl, CUtensorMap{});
+  M->map_rows.assign(2 * nl, 0);
+  M->map_ok.assign(nl, 0);
   M->maps_base = M->F;
   EncodeTiledFn enc = encode_tiled_fn();
   if (!enc) return;
   float* F = reinterpret_cast<float*>(M->F);
-  for (size_t l = 0; l < S.levels.size(); ++l) {
+  for (size_t l = 0; l < nl; ++l) {
     const MFLevel& L = S.levels[l];
     if (L.n < TS_ROWS || L.count > (1 << 16)) continue;
-    const cuuint64_t dims[3] = {(cuuint64_t)L.n, (cuuint64_t)L.n, (cuuint64_t)L.count};
-    const cuuint64_t strides[2] = {(cuuint64_t)L.n * sizeof(float), (cuuint64_t)L.n * L.n * sizeof(float)};
-    const cuuint32_t box[3] = {TS_ROWS, TS_COLS, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    if (enc(&M->maps[l], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, F + L.off, dims, strides, box, estr,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
-      M->map_ok[l] = 1;
+    bool ok = true;
+    for (int dir = 0; dir < 2; ++dir) {  // 0: forward (B rows), 1: backward (E rows)
+      const int rows = tma_rows(dir == 0 ? std::max(L.B, 1) : L.E);
+      const cuuint64_t dims[3] = {(cuuint64_t)L.n, (cuuint64_t)L.n, (cuuint64_t)L.count};
+      const cuuint64_t strides[2] = {(cuuint64_t)L.n * sizeof(float), (cuuint64_t)L.n * L.n * sizeof(float)};
+      const cuuint32_t box[3] = {(cuuint32_t)rows, TS_COLS, 1};
+      const cuuint32_t estr[3] = {1, 1, 1};
+      ok = ok && enc(&M->maps[2 * l + dir], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, F + L.off, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+      M->map_rows[2 * l + dir] = rows;
+    }
+    M->map_ok[l] = ok ? 1 : 0;
   }
 }
 
 // Column chunk of the TMA sweeps: a multiple of TS_COLS, about two waves of three resident
 // CTAs per SM for the level.
-static int tma_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t fronts) {
-  const int64_t per_chunk = std::max<int64_t>(1, (rows + TS_ROWS - 1) / TS_ROWS) * std::max<int64_t>(1, fronts);
+static int tma_cols(const gbmhd_ctx* ctx, int64_t rows, int tile_rows, int64_t ncols, int64_t fronts) {
+  const int64_t per_chunk = std::max<int64_t>(1, (rows + tile_rows - 1) / tile_rows) * std::max<int64_t>(1, fronts);
   const int64_t want = (int64_t)ctx->num_sms * 6;
   const int64_t chunks = std::max<int64_t>(1, (want + per_chunk - 1) / per_chunk);
   int64_t cols = (ncols + chunks - 1) / chunks;
@@ -1101,11 +1119,12 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first, L.E); gbmhd::count_launch(); }
     if (L.B > 0) {
       if (!tr && sizeof(T) == 4 && M->map_ok[l]) {
-        const int cw = tma_cols(ctx, L.B, L.E, cnt);
-        dim3 g((unsigned)((L.B + TS_ROWS - 1) / TS_ROWS), (unsigned)((L.E + cw - 1) / cw), (unsigned)cnt);
-        const size_t sm = TS_TILE_BYTES + sizeof(float2) * cw;
+        const int rows = M->map_rows[2 * l];
+        const int cw = tma_cols(ctx, L.B, rows, L.E, cnt);
+        dim3 g((unsigned)((L.B + rows - 1) / rows), (unsigned)((L.E + cw - 1) / cw), (unsigned)cnt);
+        const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
         MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        { k_sweep_tma<true><<<g, TS_THREADS, sm, ctx->stream>>>(M->maps[l], L.first, L.E, cw, 0, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, M->d_sweep_err); gbmhd::count_launch(); }
+        { k_sweep_tma<true><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l], L.first, L.E, rows, cw, 0, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, M->d_sweep_err); gbmhd::count_launch(); }
       } else if (!tr) {
         const int cols = sweep_cols(ctx, L.B, L.E, cnt, rows_cta);
         dim3 g((unsigned)((L.B + rows_cta - 1) / rows_cta), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
@@ -1124,12 +1143,13 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count;
     if (!tr && sizeof(T) == 4 && M->map_ok[l]) {
-      const int cw = tma_cols(ctx, L.E, L.n, cnt);
+      const int rows = M->map_rows[2 * l + 1];
+      const int cw = tma_cols(ctx, L.E, rows, L.n, cnt);
       const int ca = (L.E + cw - 1) / cw, cb = (L.B + cw - 1) / cw;
-      dim3 g((unsigned)((L.E + TS_ROWS - 1) / TS_ROWS), (unsigned)(ca + cb), (unsigned)cnt);
-      const size_t sm = TS_TILE_BYTES + sizeof(float2) * cw;
+      dim3 g((unsigned)((L.E + rows - 1) / rows), (unsigned)(ca + cb), (unsigned)cnt);
+      const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
       MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      { k_sweep_tma<false><<<g, TS_THREADS, sm, ctx->stream>>>(M->maps[l], L.first, L.E, cw, ca, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, M->d_sweep_err); gbmhd::count_launch(); }
+      { k_sweep_tma<false><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l + 1], L.first, L.E, rows, cw, ca, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, M->d_sweep_err); gbmhd::count_launch(); }
       { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
     } else if (!tr) {
       const int cols = sweep_cols(ctx, L.E, L.n, cnt, rows_cta);
