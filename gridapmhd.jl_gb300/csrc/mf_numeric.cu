@@ -11,7 +11,8 @@ using namespace gbmhd;
 
 namespace {
 
-constexpr int NB = 64;  // Gauss-Jordan pivot block
+constexpr int NB = 64;   // Gauss-Jordan pivot block (inverted by one CTA)
+constexpr int PW = 128;  // panel: the trailing part of a front is updated once per PW pivots
 
 struct DevSym {
   int32_t* f_ne = nullptr;
@@ -45,6 +46,8 @@ struct MFNumeric {
   void* Cbuf = nullptr;        // column blocks   [count][n*NB]
   void* Tbuf = nullptr;        // row blocks      [count][NB*n]
   void* T2buf = nullptr;
+  void* Rbuf = nullptr;        // panel rows before elimination   [count][PW*n]
+  void* Nbuf = nullptr;        // eliminated panel columns        [count][n*PW]
   size_t work_bytes = 0;
   double* tsave = nullptr;     // forward-sweep values of the eliminated dofs
   double* ybuf = nullptr;      // backward-sweep accumulators (kept zero between solves)
@@ -188,7 +191,7 @@ void mf_destroy(MFNumeric* M) {
   if (!M) return;
   void* ptrs[] = {M->d.f_ne, M->d.f_nb, M->d.f_off, M->d.elim_ptr, M->d.bnd_ptr, M->d.elim, M->d.bnd,
                   M->d.ah_src, M->d.ah_dst, M->d.child_list, M->d.ea_ptr, M->d.ea_pos, M->d.f_parent,
-                  M->d.f_level, M->d.reg_dst, M->d.reg_dof, M->F, M->Pbuf, M->Cbuf, M->Tbuf, M->T2buf, M->tsave, M->ybuf, M->tsave_off, M->d_err};
+                  M->d.f_level, M->d.reg_dst, M->d.reg_dof, M->F, M->Pbuf, M->Cbuf, M->Tbuf, M->T2buf, M->Rbuf, M->Nbuf, M->tsave, M->ybuf, M->tsave_off, M->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (M->blas) cublasDestroy(M->blas);
@@ -454,37 +457,63 @@ __global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restric
     Pf[ti + j * NB] = (ti < kb && j < kb) ? __fadd_rn(Ah[ti + colsrc[j] * kb], Al[ti + colsrc[j] * kb]) : 0.0f;
 }
 
-// C = M[0:w, K] with the K rows zeroed; Tb = M[K, 0:w]  (both per front; w = E: the
-// Gauss-Jordan sweep runs over the pivot block F11 only).  Grid (column groups, fronts).
+// C = M[:, K] with the K rows zeroed (n x kb); Tb = M[K, c0 : c0+cw] (kb x cw).  Grid
+// (column groups, fronts).
 template <typename T>
-__global__ void __launch_bounds__(256) k_gj_copy(const T* __restrict__ F, int64_t off, int n, int w, int k, int kb,
-                                                 T* __restrict__ C, T* __restrict__ Tb) {
+__global__ void __launch_bounds__(256) k_gj_copy(const T* __restrict__ F, int64_t off, int n, int k, int kb, int c0,
+                                                 int cw, T* __restrict__ C, T* __restrict__ Tb) {
   const int64_t f = blockIdx.y;
   const T* M = F + off + f * (int64_t)n * n;
   T* Cf = C + f * (int64_t)n * NB;
   T* Tf = Tb + f * (int64_t)NB * n;
-  for (int j = blockIdx.x; j < kb; j += gridDim.x)  // C: w rows of column k + j
-    for (int i = threadIdx.x; i < w; i += blockDim.x)
+  for (int j = blockIdx.x; j < kb; j += gridDim.x)  // C: column k + j
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
       Cf[i + (int64_t)j * n] = (i >= k && i < k + kb) ? (T)0 : M[i + (int64_t)(k + j) * n];
   const int r = threadIdx.x & (NB - 1);
-  for (int c = blockIdx.x * (256 / NB) + threadIdx.x / NB; c < w; c += gridDim.x * (256 / NB))  // Tb: kb rows
-    if (r < kb) Tf[r + (int64_t)c * NB] = M[(k + r) + (int64_t)c * n];
+  for (int c = blockIdx.x * (256 / NB) + threadIdx.x / NB; c < cw; c += gridDim.x * (256 / NB))  // Tb: kb rows
+    if (r < kb) Tf[r + (int64_t)c * NB] = M[(k + r) + (int64_t)(c0 + c) * n];
 }
 
-// M[K, c] = T2[:, c] for c < w outside K; M[K, K] = P.
+// M[K, c0 + c] = T2[:, c] for c < cw outside K; M[K, K] = P.
 template <typename T>
-__global__ void __launch_bounds__(256) k_gj_fix(T* __restrict__ F, int64_t off, int n, int w, int k, int kb,
+__global__ void __launch_bounds__(256) k_gj_fix(T* __restrict__ F, int64_t off, int n, int k, int kb, int c0, int cw,
                                                 const T* __restrict__ T2, const T* __restrict__ P) {
   const int64_t f = blockIdx.y;
   T* M = F + off + f * (int64_t)n * n;
   const T* T2f = T2 + f * (int64_t)NB * n;
   const T* Pf = P + f * (int64_t)NB * NB;
   const int r = threadIdx.x & (NB - 1);
-  for (int c = blockIdx.x * (256 / NB) + threadIdx.x / NB; c < w; c += gridDim.x * (256 / NB))
+  for (int c = blockIdx.x * (256 / NB) + threadIdx.x / NB; c < cw; c += gridDim.x * (256 / NB))
     if (r < kb) {
-      const bool inK = c >= k && c < k + kb;
-      M[(k + r) + (int64_t)c * n] = inK ? Pf[r + (int64_t)(c - k) * NB] : T2f[r + (int64_t)c * NB];
+      const int cc = c0 + c;
+      const bool inK = cc >= k && cc < k + kb;
+      M[(k + r) + (int64_t)cc * n] = inK ? Pf[r + (int64_t)(cc - k) * NB] : T2f[r + (int64_t)c * NB];
     }
+}
+
+// Panel elimination helpers (panel = pivot columns [p, p + pw)):
+// R = M[p : p+pw, :] (pw x n, ld PW) before the panel is eliminated, and Nz = M[:, p : p+pw]
+// with the panel rows zeroed (n x pw, ld n) after it.
+template <typename T>
+__global__ void __launch_bounds__(256) k_panel_rows(const T* __restrict__ F, int64_t off, int n, int p, int pw,
+                                                    T* __restrict__ R) {
+  const int64_t f = blockIdx.y;
+  const T* M = F + off + f * (int64_t)n * n;
+  T* Rf = R + f * (int64_t)PW * n;
+  const int r = threadIdx.x & (PW - 1);
+  for (int c = blockIdx.x * (256 / PW) + threadIdx.x / PW; c < n; c += gridDim.x * (256 / PW))
+    if (r < pw) Rf[r + (int64_t)c * PW] = M[(p + r) + (int64_t)c * n];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_panel_cols(const T* __restrict__ F, int64_t off, int n, int p, int pw,
+                                                    T* __restrict__ Nz) {
+  const int64_t f = blockIdx.y;
+  const T* M = F + off + f * (int64_t)n * n;
+  T* Nf = Nz + f * (int64_t)n * PW;
+  for (int j = blockIdx.x; j < pw; j += gridDim.x)
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      Nf[i + (int64_t)j * n] = (i >= p && i < p + pw) ? (T)0 : M[i + (int64_t)(p + j) * n];
 }
 
 // ------------------------------------------------------------------ solve kernels
@@ -989,18 +1018,23 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
     MF_CUDA(cudaMalloc(&M->F, fbytes));
     M->F_bytes = fbytes;
   }
-  size_t wmax = 0;
-  for (const MFLevel& L : S.levels) wmax = std::max(wmax, (size_t)L.count * L.n * NB);
+  size_t wmax = 0, pmax = 0;
+  for (const MFLevel& L : S.levels) {
+    wmax = std::max(wmax, (size_t)L.count * L.n * NB);
+    pmax = std::max(pmax, (size_t)L.count * L.n * PW);
+  }
   size_t pbytes = 0;
   for (const MFLevel& L : S.levels) pbytes = std::max(pbytes, (size_t)L.count * NB * NB);
-  const size_t need = sizeof(T) * (3 * wmax + pbytes);
+  const size_t need = sizeof(T) * (3 * wmax + pbytes + 2 * pmax);
   if (M->work_bytes < need) {
-    for (void* p : {M->Pbuf, M->Cbuf, M->Tbuf, M->T2buf})
+    for (void* p : {M->Pbuf, M->Cbuf, M->Tbuf, M->T2buf, M->Rbuf, M->Nbuf})
       if (p) cudaFree(p);
     MF_CUDA(cudaMalloc(&M->Pbuf, sizeof(T) * std::max<size_t>(pbytes, 1)));
     MF_CUDA(cudaMalloc(&M->Cbuf, sizeof(T) * std::max<size_t>(wmax, 1)));
     MF_CUDA(cudaMalloc(&M->Tbuf, sizeof(T) * std::max<size_t>(wmax, 1)));
     MF_CUDA(cudaMalloc(&M->T2buf, sizeof(T) * std::max<size_t>(wmax, 1)));
+    MF_CUDA(cudaMalloc(&M->Rbuf, sizeof(T) * std::max<size_t>(pmax, 1)));
+    MF_CUDA(cudaMalloc(&M->Nbuf, sizeof(T) * std::max<size_t>(pmax, 1)));
     M->work_bytes = need;
   }
   T* F = reinterpret_cast<T*>(M->F);
@@ -1008,6 +1042,8 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
   T* C = reinterpret_cast<T*>(M->Cbuf);
   T* Tb = reinterpret_cast<T*>(M->Tbuf);
   T* T2 = reinterpret_cast<T*>(M->T2buf);
+  T* R = reinterpret_cast<T*>(M->Rbuf);
+  T* Nz = reinterpret_cast<T*>(M->Nbuf);
   MF_CUDA(cudaMemsetAsync(M->d_err, 0, sizeof(int32_t), ctx->stream));
   // level sizes on the device for the extend-add kernel
   std::vector<int> ln(S.levels.size()), le(S.levels.size());
@@ -1044,30 +1080,57 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
                                                      M->d.f_parent, M->d.f_level, M->d.ea_ptr, M->d.ea_pos, d_ln, d_le); gbmhd::count_launch(); }
     }
     MF_CUDA(cudaGetLastError());
-    // Blocked in-place Gauss-Jordan over the eliminated pivots: every 64-pivot step updates
-    // the whole front, so F12, F21 and S are formed by the same progressive elimination as
-    // F11⁻¹.  (Forming them afterwards from the FP32 F11⁻¹ with three large GEMMs multiplies
-    // the inverse's rounding by κ(F11): at Ha = 500 that tripled the FGMRES iterations.)
-    for (int k = 0; k < E; k += NB) {
-      const int kb = std::min(NB, E - k);
-      if constexpr (sizeof(T) == 4)
-        { k_pivot_inverse_df<<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
-      else
-        { k_pivot_inverse<T><<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
-      dim3 gc((unsigned)std::max(kb, (n + 3) / 4), (unsigned)cnt);
-      { k_gj_copy<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, n, k, kb, C, Tb); gbmhd::count_launch(); }
+    // Blocked in-place Gauss-Jordan over the eliminated pivots, by panels of PW pivots.
+    // Inside a panel, each 64-pivot block is eliminated from the panel's columns only (its
+    // inverse from k_pivot_inverse*, three small GEMMs); the rest of the front then takes the
+    // whole panel's elimination in one rank-PW update: M[:, rest] += Nz·R, M[P, rest] = N[P]·R
+    // (R = the panel rows before, N = the panel columns after).  Every pivot block still
+    // updates the whole front before the next panel, so F12, F21 and S come from the same
+    // progressive elimination as F11⁻¹.  (Forming them afterwards from the FP32 F11⁻¹ with
+    // three large GEMMs multiplies the inverse's rounding by κ(F11): at Ha = 500 that tripled
+    // the FGMRES iterations.)  One pass over a front per PW pivots instead of per 64 halves
+    // the HBM traffic of these memory-bound updates.
+    for (int p = 0; p < E; p += PW) {
+      const int pw = std::min(PW, E - p);
+      dim3 gr((unsigned)((n + 1) / 2), (unsigned)cnt);
+      { k_panel_rows<T><<<gr, 256, 0, ctx->stream>>>(F, L.off, n, p, pw, R); gbmhd::count_launch(); }
+      for (int k = p; k < p + pw; k += NB) {
+        const int kb = std::min(NB, p + pw - k);
+        if constexpr (sizeof(T) == 4)
+          { k_pivot_inverse_df<<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
+        else
+          { k_pivot_inverse<T><<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
+        dim3 gc((unsigned)std::max(kb, (pw + 3) / 4), (unsigned)cnt);
+        { k_gj_copy<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, p, pw, C, Tb); gbmhd::count_launch(); }
+        MF_CUDA(cudaGetLastError());
+        // T2 = P · Tb  (kb x pw)
+        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, kb, pw, kb, &one, P, NB, (long long)NB * NB, Tb,
+                           NB, (long long)NB * n, &zero, T2, NB, (long long)NB * n, cnt));
+        // M[:, panel] -= C · T2   (n x pw)
+        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, pw, kb, &mone, C, n, (long long)n * NB, T2,
+                           NB, (long long)NB * n, &one, F + L.off + (int64_t)p * n, n, (long long)n * n, cnt));
+        // M[:, K] = −C · P  (n x kb)
+        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, kb, kb, &mone, C, n, (long long)n * NB, P,
+                           NB, (long long)NB * NB, &zero, F + L.off + (int64_t)k * n, n, (long long)n * n, cnt));
+        { k_gj_fix<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, p, pw, T2, P); gbmhd::count_launch(); }
+        MF_CUDA(cudaGetLastError());
+      }
+      dim3 gn((unsigned)pw, (unsigned)cnt);
+      { k_panel_cols<T><<<gn, 256, 0, ctx->stream>>>(F, L.off, n, p, pw, Nz); gbmhd::count_launch(); }
       MF_CUDA(cudaGetLastError());
-      // T2 = P · Tb  (kb x n)
-      gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, kb, n, kb, &one, P, NB, (long long)NB * NB, Tb, NB,
-                         (long long)NB * n, &zero, T2, NB, (long long)NB * n, cnt));
-      // M -= C · T2   (n x n)
-      gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, n, kb, &mone, C, n, (long long)n * NB, T2, NB,
-                         (long long)NB * n, &one, F + L.off, n, (long long)n * n, cnt));
-      // M[:, K] = −C · P  (n x kb)
-      gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, kb, kb, &mone, C, n, (long long)n * NB, P, NB,
-                         (long long)NB * NB, &zero, F + L.off + (int64_t)k * n, n, (long long)n * n, cnt));
-      { k_gj_fix<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, n, k, kb, T2, P); gbmhd::count_launch(); }
-      MF_CUDA(cudaGetLastError());
+      // rest = columns [0, p) and [p + pw, n)
+      for (int side = 0; side < 2; ++side) {
+        const int c0 = side == 0 ? 0 : p + pw, cw = side == 0 ? p : n - (p + pw);
+        if (cw <= 0) continue;
+        // M[:, rest] += Nz · R[:, rest]   (n x cw, inner pw)
+        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, cw, pw, &one, Nz, n, (long long)n * PW,
+                           R + (int64_t)c0 * PW, PW, (long long)PW * n, &one, F + L.off + (int64_t)c0 * n, n,
+                           (long long)n * n, cnt));
+        // M[P, rest] = N[P, :] · R[:, rest]   (pw x cw; N[P, :] = the panel's pivot-block inverse)
+        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, pw, cw, pw, &one,
+                           F + L.off + p + (int64_t)p * n, n, (long long)n * n, R + (int64_t)c0 * PW, PW,
+                           (long long)PW * n, &zero, F + L.off + p + (int64_t)c0 * n, n, (long long)n * n, cnt));
+      }
     }
   }
   MF_CUDA(cudaFreeAsync(d_ln, ctx->stream));

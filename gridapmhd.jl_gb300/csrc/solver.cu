@@ -690,9 +690,14 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
   bool factored = false;
   int status = 1;
   // In GBMHD_MIXED the operator starts as the FP32 Jacobian (Newton with an FP32 Jacobian is
-  // iterative refinement with an FP64 residual).  When that refinement stops contracting
-  // (‖r_k‖ > 0.1‖r_{k-1}‖), the operator switches to the FP64 Jacobian; the FP32 factors stay.
+  // iterative refinement with an FP64 residual).  When a step contracts the residual by less
+  // than a tenth of what its linear solve asked for (‖r_k‖ > max(10 linear_rtol, 1e-2)
+  // ‖r_{k-1}‖), the FP32 operator's own error is the limit: the operator switches to the FP64
+  // Jacobian; the FP32 factors stay.  With the FP64 operator a linear solve reduces the
+  // Newton residual by about its tolerance, so each such step asks for just the reduction
+  // that reaches the stopping target (never less than linear_rtol).
   int op_prec = prec;
+  const double switch_ratio = std::max(10.0 * o->linear_rtol, 1e-2);
   for (int it = 0;; ++it) {
     double ta = now_s();
     if ((rc = gb_assemble_device(ctx, d_x, r, 0, op_prec))) return rc;
@@ -711,7 +716,7 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     // attainable-accuracy stop (FP64 operator only): the FP64 residual no longer decreases
     if (it >= 2 && op_prec == GBMHD_FP64 && rn > 0.9 * prev && rn <= 1e-9 * r0) { status = 0; break; }
     if (it >= o->max_newton) break;
-    if (op_prec == GBMHD_MIXED && it >= 1 && rn > 0.1 * prev) {
+    if (op_prec == GBMHD_MIXED && it >= 1 && rn > switch_ratio * prev) {
       op_prec = GBMHD_FP64;
       if (!ctx->d_val64) S_CUDA(cudaMalloc(&ctx->d_val64, sizeof(double) * ctx->nnz));
       if (o->verbose) std::fprintf(stderr, "  operator: FP64 Jacobian from here on\n");
@@ -731,7 +736,10 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     if ((rc = ensure_workspace(ctx, o->restart))) return rc;
     { k_scale_copy<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, -1.0, r, ctx->d_xtmp); gbmhd::count_launch(); }
     // b = −r lives in d_xtmp; solution into r (reused as δ)
-    if ((rc = fgmres(ctx, op_prec, ctx->d_xtmp, r, o->restart, o->max_linear, o->linear_rtol, false, &iters, &rel,
+    double lin_rtol = o->linear_rtol;
+    if (op_prec == GBMHD_FP64 && rn > 0.0)
+      lin_rtol = std::min(o->linear_rtol, std::max(0.5 * std::max(o->newton_atol, o->newton_rtol * r0) / rn, 1e-10));
+    if ((rc = fgmres(ctx, op_prec, ctx->d_xtmp, r, o->restart, o->max_linear, lin_rtol, false, &iters, &rel,
                      o->verbose)))
       return rc;
     R.linear_iters += iters;
