@@ -628,6 +628,32 @@ __device__ __forceinline__ void strided_dot_rows(SweepAcc<T> (&acc)[RowVec<T>::R
   }
 }
 
+// acc += Σ_{i<len} col[i] v[i] for one warp: lanes read 16-byte groups of four rows, sum the
+// products of four groups (16 terms) with FP32 FMAs (vector high and low parts separately)
+// and fold those short sums into the float-float accumulator.  col must be 16-byte aligned
+// and v zero-padded to a multiple of 4.
+__device__ __forceinline__ void warp_col_dot(SweepAcc<float>& acc, const float* __restrict__ col,
+                                             const float2* __restrict__ v, int len, int lane) {
+  const int len4 = (len + 3) >> 2;
+  const float4* c4 = reinterpret_cast<const float4*>(col);
+  for (int g0 = 0; g0 < len4; g0 += 128) {
+    float h = 0.0f, l = 0.0f;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int g = g0 + lane + 32 * u;
+      if (g < len4) {
+        const float4 m = __ldcs(c4 + g);
+        const float2 v0 = v[4 * g], v1 = v[4 * g + 1], v2 = v[4 * g + 2], v3 = v[4 * g + 3];
+        h = fmaf(m.x, v0.x, h); l = fmaf(m.x, v0.y, l);
+        h = fmaf(m.y, v1.x, h); l = fmaf(m.y, v1.y, l);
+        h = fmaf(m.z, v2.x, h); l = fmaf(m.z, v2.y, l);
+        h = fmaf(m.w, v3.x, h); l = fmaf(m.w, v3.y, l);
+      }
+    }
+    acc.merge(h, l);
+  }
+}
+
 // Transposed sweeps (adjoint solves), one warp per column: each dot product runs down a
 // contiguous column of the column-major front.
 // forward, transposed: b[bnd_j] −= Σ_{i<ne} TR[i, j] t_i   (TR = rows 0..E of column E+j)
@@ -643,14 +669,19 @@ __global__ void __launch_bounds__(256) k_fwd_gemv_t(const T* __restrict__ F, con
   const int64_t f = first + blockIdx.y;
   const int nb = f_nb[f], ne = f_ne[f];
   const double* t = tsave + toff[f];
-  for (int i = threadIdx.x; i < ne; i += blockDim.x) ts[i] = SweepAcc<T>::pack(t[i]);
+  const int ne4 = (ne + 3) & ~3;  // zero padding to the 16-byte groups (ne4 <= E)
+  for (int i = threadIdx.x; i < ne4; i += blockDim.x) ts[i] = SweepAcc<T>::pack(i < ne ? t[i] : 0.0);
   __syncthreads();
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int j = blockIdx.x * (blockDim.x / 32) + warp;
   if (j >= nb) return;
   const T* colj = F + f_off[f] + (int64_t)(E + j) * n;
   SweepAcc<T> acc;
-  for (int i = lane; i < ne; i += 32) acc.add(colj[i], ts[i]);
+  if constexpr (sizeof(T) == 4) {
+    warp_col_dot(acc, colj, ts, ne, lane);
+  } else {
+    for (int i = lane; i < ne; i += 32) acc.add(colj[i], ts[i]);
+  }
   acc.warp_reduce();
   if (lane == 0) atomicAdd(&b[bnd[bnd_ptr[f] + j]], -acc.value());
 }
@@ -671,16 +702,22 @@ __global__ void __launch_bounds__(256) k_bwd_gemv_t(const T* __restrict__ F, con
   const int ne = f_ne[f], nb = f_nb[f];
   const double* t = tsave + toff[f];
   const int32_t* bd = bnd + bnd_ptr[f];
-  for (int i = threadIdx.x; i < ne; i += blockDim.x) vs[i] = SweepAcc<T>::pack(t[i]);
-  for (int j = threadIdx.x; j < nb; j += blockDim.x) vs[E + j] = SweepAcc<T>::pack(x[bd[j]]);
+  const int ne4 = (ne + 3) & ~3, nb4 = (nb + 3) & ~3;  // zero padding (ne4 <= E, E + nb4 <= n)
+  for (int i = threadIdx.x; i < ne4; i += blockDim.x) vs[i] = SweepAcc<T>::pack(i < ne ? t[i] : 0.0);
+  for (int j = threadIdx.x; j < nb4; j += blockDim.x) vs[E + j] = SweepAcc<T>::pack(j < nb ? x[bd[j]] : 0.0);
   __syncthreads();
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int i = blockIdx.x * (blockDim.x / 32) + warp;
   if (i >= ne) return;
   const T* coli = F + f_off[f] + (int64_t)i * n;
   SweepAcc<T> acc;
-  for (int c = lane; c < ne; c += 32) acc.add(coli[c], vs[c]);
-  for (int j = lane; j < nb; j += 32) acc.add(coli[E + j], vs[E + j]);
+  if constexpr (sizeof(T) == 4) {
+    warp_col_dot(acc, coli, vs, ne, lane);
+    warp_col_dot(acc, coli + E, vs + E, nb, lane);
+  } else {
+    for (int c = lane; c < ne; c += 32) acc.add(coli[c], vs[c]);
+    for (int j = lane; j < nb; j += 32) acc.add(coli[E + j], vs[E + j]);
+  }
   acc.warp_reduce();
   if (lane == 0) x[elim[elim_ptr[f] + i]] = acc.value();
 }
@@ -866,13 +903,22 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
       const float* tile = tiles + (size_t)buf * TS_COLS * rows;
       const float2* vv = vs + s * TS_COLS;
       const int cn = min(TS_COLS, ncol - s * TS_COLS);
+      // a stage's (at most 16) products are summed with FP32 FMAs, the high and low parts of
+      // the vector separately, and the two short sums are folded into the float-float
+      // accumulators: ~3 instructions per factor entry instead of ~13 for float-float per
+      // product, with the rounding of 16-term FP32 sums only
+      float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f;
 #pragma unroll 4
       for (int c = 0; c < cn; ++c) {
         const float2 m = *reinterpret_cast<const float2*>(tile + c * rows + r);
         const float2 v = vv[c];
-        a0.add(m.x, v);
-        a1.add(m.y, v);
+        h0 = fmaf(m.x, v.x, h0);
+        l0 = fmaf(m.x, v.y, l0);
+        h1 = fmaf(m.y, v.x, h1);
+        l1 = fmaf(m.y, v.y, l1);
       }
+      a0.merge(h0, l0);
+      a1.merge(h1, l1);
     } else {
       abort_flag = 1;
     }

@@ -716,7 +716,9 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     // attainable-accuracy stop (FP64 operator only): the FP64 residual no longer decreases
     if (it >= 2 && op_prec == GBMHD_FP64 && rn > 0.9 * prev && rn <= 1e-9 * r0) { status = 0; break; }
     if (it >= o->max_newton) break;
-    if (op_prec == GBMHD_MIXED && it >= 1 && rn > switch_ratio * prev) {
+    // also switch once the residual is within FP32 resolution of r0: the FP32 operator's own
+    // rounding cannot resolve a smaller residual
+    if (op_prec == GBMHD_MIXED && ((it >= 1 && rn > switch_ratio * prev) || rn <= 1e-6 * r0)) {
       op_prec = GBMHD_FP64;
       if (!ctx->d_val64) S_CUDA(cudaMalloc(&ctx->d_val64, sizeof(double) * ctx->nnz));
       if (o->verbose) std::fprintf(stderr, "  operator: FP64 Jacobian from here on\n");
