@@ -358,8 +358,11 @@ __device__ __forceinline__ void df_rcp(float ah, float al, float& h, float& l) {
 
 __global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restrict__ F, int64_t off, int n, int k,
                                                           int kb, float* __restrict__ P, int32_t* err) {
-  __shared__ float Ah[NB * NB], Al[NB * NB];  // column-major, ld kb
-  __shared__ float rh[NB], rl[NB], mh[NB], ml[NB];
+  // column-major with leading dimension LD = NB + 1: row accesses (swap, pivot row) are
+  // free of bank conflicts
+  constexpr int LD = NB + 1;
+  __shared__ float Ah[NB * LD], Al[NB * LD];
+  __shared__ float rh[NB], rl[NB], mh[NB], ml[NB], ch[NB], cl[NB];
   __shared__ int perm[NB], colsrc[NB];
   __shared__ int piv_row;
   const int64_t f = blockIdx.x;
@@ -369,17 +372,21 @@ __global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restric
   constexpr int CG = 256 / NB;
   if (ti < kb)
     for (int j = tj; j < kb; j += CG) {
-      Ah[ti + j * kb] = M[(k + ti) + (int64_t)(k + j) * n];
-      Al[ti + j * kb] = 0.0f;
+      Ah[ti + j * LD] = M[(k + ti) + (int64_t)(k + j) * n];
+      Al[ti + j * LD] = 0.0f;
     }
   __syncthreads();
   for (int c = 0; c < kb; ++c) {
-    if (tid < 32) {  // argmax |A[i, c]| (high parts) over rows c..kb-1 (ties: the lower row)
+    // (1) warp 0: argmax |A[i, c]| (high parts) over rows c..kb-1 (ties: the lower row), and
+    //     a copy of column c, so that (2) can swap rows while reading the old column
+    if (tid < 32) {
       float best = -1.0f;
       int bi = c;
-      for (int i = c + tid; i < kb; i += 32) {
-        const float a = fabsf(Ah[i + c * kb]);
-        if (a > best) { best = a; bi = i; }
+      for (int i = tid; i < kb; i += 32) {
+        const float h = Ah[i + c * LD];
+        ch[i] = h;
+        cl[i] = Al[i + c * LD];
+        if (i >= c && fabsf(h) > best) { best = fabsf(h); bi = i; }
       }
       for (int o = 16; o > 0; o >>= 1) {
         const float ob = __shfl_down_sync(0xffffffffu, best, o);
@@ -393,38 +400,43 @@ __global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restric
       }
     }
     __syncthreads();
+    // (2) thread j < kb: swap rows c and pr of column j, scale the new row c by 1 / pivot;
+    //     multipliers m_i = A[i, c] after the swap (from the copy of column c)
     const int pr = piv_row;
-    if (pr != c && tid < kb) {
-      float t = Ah[c + tid * kb];
-      Ah[c + tid * kb] = Ah[pr + tid * kb];
-      Ah[pr + tid * kb] = t;
-      t = Al[c + tid * kb];
-      Al[c + tid * kb] = Al[pr + tid * kb];
-      Al[pr + tid * kb] = t;
-    }
-    __syncthreads();
     if (tid < kb) {
-      float ih = 0.0f, il = 0.0f;  // 1 / A[c, c] in float-float
-      const float dh = Ah[c + c * kb], dl = Al[c + c * kb];
+      const int j = tid;
+      float ih = 0.0f, il = 0.0f;
+      const float dh = ch[pr], dl = cl[pr];  // the pivot
       if (dh != 0.0f) df_rcp(dh, dl, ih, il);
-      if (tid == c) { rh[tid] = ih; rl[tid] = il; }
-      else df_mul(Ah[c + tid * kb], Al[c + tid * kb], ih, il, rh[tid], rl[tid]);
-      if (tid == c) { mh[tid] = 0.0f; ml[tid] = 0.0f; }
-      else { mh[tid] = Ah[tid + c * kb]; ml[tid] = Al[tid + c * kb]; }
+      const float ah = Ah[pr + j * LD], al = Al[pr + j * LD];  // new row c, column j
+      if (pr != c) {
+        Ah[pr + j * LD] = Ah[c + j * LD];
+        Al[pr + j * LD] = Al[c + j * LD];
+      }
+      if (j == c) { rh[j] = ih; rl[j] = il; }
+      else df_mul(ah, al, ih, il, rh[j], rl[j]);
+      const int i = tid;
+      const int src = i == pr ? c : i;  // row i after the swap holds the old row src
+      if (i == c) { mh[i] = 0.0f; ml[i] = 0.0f; }
+      else { mh[i] = ch[src]; ml[i] = cl[src]; }
     }
     __syncthreads();
+    // (3) rank-1 update of every row but c; row c becomes the scaled pivot row
     if (ti < kb) {
       const float m_h = mh[ti], m_l = ml[ti];
-      for (int j = tj; j < kb; j += CG) {
-        const int idx = ti + j * kb;
+#pragma unroll
+      for (int u = 0; u < NB / CG; ++u) {
+        const int j = tj + u * CG;
+        if (j >= kb) break;
+        const int idx = ti + j * LD;
+        const float r_h = rh[j], r_l = rl[j];
         if (ti == c) {
-          Ah[idx] = rh[j];
-          Al[idx] = rl[j];
+          Ah[idx] = r_h;
+          Al[idx] = r_l;
           continue;
         }
         const float ah = j == c ? 0.0f : Ah[idx], al = j == c ? 0.0f : Al[idx];
         // p = m · r in float-float
-        const float r_h = rh[j], r_l = rl[j];
         const float ph = __fmul_rn(m_h, r_h);
         float pl = fmaf(m_h, r_h, -ph);
         pl = fmaf(m_h, r_l, pl);
@@ -454,7 +466,7 @@ __global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restric
   __syncthreads();
   float* Pf = P + f * (int64_t)NB * NB;
   for (int j = tj; j < NB; j += CG)  // column-major, zero outside kb x kb
-    Pf[ti + j * NB] = (ti < kb && j < kb) ? __fadd_rn(Ah[ti + colsrc[j] * kb], Al[ti + colsrc[j] * kb]) : 0.0f;
+    Pf[ti + j * NB] = (ti < kb && j < kb) ? __fadd_rn(Ah[ti + colsrc[j] * LD], Al[ti + colsrc[j] * LD]) : 0.0f;
 }
 
 // C = M[:, K] with the K rows zeroed (n x kb); Tb = M[K, c0 : c0+cw] (kb x cw).  Grid
