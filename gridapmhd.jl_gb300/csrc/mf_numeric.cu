@@ -60,6 +60,7 @@ struct MFNumeric {
   std::vector<int> map_rows;      // row tile of each map
   std::vector<char> map_ok;
   const void* maps_base = nullptr;
+  float2* vpk = nullptr;            // packed vector segments of one level (transposed sweeps)
   int32_t* d_sweep_err = nullptr;   // set by a sweep whose TMA wait timed out
   int32_t* h_sweep_err = nullptr;   // pinned copy, read at the next solve
   // sweep timing: events around each solve, harvested when the next one starts
@@ -162,6 +163,11 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
     const int64_t ne = S.f_ne[f], nb = S.f_nb[f];
     M->sweep_elems += nb * ne + ne * (ne + nb);
   }
+  {
+    size_t vmax = 1;
+    for (const MFLevel& L : S.levels) vmax = std::max(vmax, (size_t)L.count * L.n);
+    MF_CUDA(cudaMalloc(&M->vpk, sizeof(float2) * vmax));
+  }
   MF_CUDA(cudaMalloc(&M->d_sweep_err, sizeof(int32_t)));
   MF_CUDA(cudaMemset(M->d_sweep_err, 0, sizeof(int32_t)));
   MF_CUDA(cudaMallocHost(&M->h_sweep_err, sizeof(int32_t)));
@@ -195,6 +201,7 @@ void mf_destroy(MFNumeric* M) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (M->blas) cublasDestroy(M->blas);
+  if (M->vpk) cudaFree(M->vpk);
   if (M->d_sweep_err) cudaFree(M->d_sweep_err);
   if (M->h_sweep_err) cudaFreeHost(M->h_sweep_err);
   if (M->ev0) cudaEventDestroy(M->ev0);
@@ -674,23 +681,25 @@ __global__ void __launch_bounds__(256) k_fwd_gemv_t(const T* __restrict__ F, con
                                                     double* __restrict__ b, const double* __restrict__ tsave,
                                                     const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
                                                     const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_nb,
-                                                    const int32_t* __restrict__ f_ne, int64_t first, int n, int E) {
+                                                    const int32_t* __restrict__ f_ne, int64_t first, int n, int E,
+                                                    const float2* __restrict__ vpk) {
   using V = typename SweepAcc<T>::V;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   V* ts = reinterpret_cast<V*>(sm_raw);
   const int64_t f = first + blockIdx.y;
   const int nb = f_nb[f], ne = f_ne[f];
-  const double* t = tsave + toff[f];
-  const int ne4 = (ne + 3) & ~3;  // zero padding to the 16-byte groups (ne4 <= E)
-  for (int i = threadIdx.x; i < ne4; i += blockDim.x) ts[i] = SweepAcc<T>::pack(i < ne ? t[i] : 0.0);
-  __syncthreads();
+  if constexpr (sizeof(T) != 4) {
+    const double* t = tsave + toff[f];
+    for (int i = threadIdx.x; i < ne; i += blockDim.x) ts[i] = SweepAcc<T>::pack(t[i]);
+    __syncthreads();
+  }
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int j = blockIdx.x * (blockDim.x / 32) + warp;
   if (j >= nb) return;
   const T* colj = F + f_off[f] + (int64_t)(E + j) * n;
   SweepAcc<T> acc;
   if constexpr (sizeof(T) == 4) {
-    warp_col_dot(acc, colj, ts, ne, lane);
+    warp_col_dot(acc, colj, vpk + (int64_t)blockIdx.y * n, ne, lane);  // packed t of this front
   } else {
     for (int i = lane; i < ne; i += 32) acc.add(colj[i], ts[i]);
   }
@@ -706,32 +715,53 @@ __global__ void __launch_bounds__(256) k_bwd_gemv_t(const T* __restrict__ F, con
                                                     const int64_t* __restrict__ toff, const int32_t* __restrict__ elim,
                                                     const int64_t* __restrict__ elim_ptr, const int32_t* __restrict__ bnd,
                                                     const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
-                                                    const int32_t* __restrict__ f_nb, int64_t first, int n, int E) {
+                                                    const int32_t* __restrict__ f_nb, int64_t first, int n, int E,
+                                                    const float2* __restrict__ vpk) {
   using V = typename SweepAcc<T>::V;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   V* vs = reinterpret_cast<V*>(sm_raw);  // [E] t, then [n-E] x_B
   const int64_t f = first + blockIdx.y;
   const int ne = f_ne[f], nb = f_nb[f];
-  const double* t = tsave + toff[f];
-  const int32_t* bd = bnd + bnd_ptr[f];
-  const int ne4 = (ne + 3) & ~3, nb4 = (nb + 3) & ~3;  // zero padding (ne4 <= E, E + nb4 <= n)
-  for (int i = threadIdx.x; i < ne4; i += blockDim.x) vs[i] = SweepAcc<T>::pack(i < ne ? t[i] : 0.0);
-  for (int j = threadIdx.x; j < nb4; j += blockDim.x) vs[E + j] = SweepAcc<T>::pack(j < nb ? x[bd[j]] : 0.0);
-  __syncthreads();
+  if constexpr (sizeof(T) != 4) {
+    const double* t = tsave + toff[f];
+    const int32_t* bd = bnd + bnd_ptr[f];
+    for (int i = threadIdx.x; i < ne; i += blockDim.x) vs[i] = SweepAcc<T>::pack(t[i]);
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) vs[E + j] = SweepAcc<T>::pack(x[bd[j]]);
+    __syncthreads();
+  }
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int i = blockIdx.x * (blockDim.x / 32) + warp;
   if (i >= ne) return;
   const T* coli = F + f_off[f] + (int64_t)i * n;
   SweepAcc<T> acc;
   if constexpr (sizeof(T) == 4) {
-    warp_col_dot(acc, coli, vs, ne, lane);
-    warp_col_dot(acc, coli + E, vs + E, nb, lane);
+    const float2* v = vpk + (int64_t)blockIdx.y * n;  // packed [t ; x_B] of this front
+    warp_col_dot(acc, coli, v, ne, lane);
+    warp_col_dot(acc, coli + E, v + E, nb, lane);
   } else {
     for (int c = lane; c < ne; c += 32) acc.add(coli[c], vs[c]);
     for (int j = lane; j < nb; j += 32) acc.add(coli[E + j], vs[E + j]);
   }
   acc.warp_reduce();
   if (lane == 0) x[elim[elim_ptr[f] + i]] = acc.value();
+}
+
+// Packed (float-float) vector segments of a level's fronts for the transposed FP32 sweeps:
+// vpk[front][0, E) = t (zero beyond ne), and with x given, vpk[front][E, n) = x_B (zero
+// beyond nb).  One pass per level instead of every CTA staging its front's segment.
+__global__ void k_pack_vec(const double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                           const double* __restrict__ x, const int32_t* __restrict__ bnd,
+                           const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
+                           const int32_t* __restrict__ f_nb, int64_t first, int n, int E, float2* __restrict__ vpk) {
+  const int64_t f = first + blockIdx.x;
+  const int ne = f_ne[f], nb = f_nb[f];
+  const double* t = tsave + toff[f];
+  float2* v = vpk + (int64_t)blockIdx.x * n;
+  for (int i = threadIdx.x; i < E; i += blockDim.x) v[i] = SweepAcc<float>::pack(i < ne ? t[i] : 0.0);
+  if (x) {
+    const int32_t* bd = bnd + bnd_ptr[f];
+    for (int j = threadIdx.x; j < n - E; j += blockDim.x) v[E + j] = SweepAcc<float>::pack(j < nb ? x[bd[j]] : 0.0);
+  }
 }
 
 // Chunked sweeps: grid (row tiles, column chunks, fronts); each thread owns R consecutive
@@ -1251,11 +1281,13 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
         dim3 g((unsigned)((L.B + rows_cta - 1) / rows_cta), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
         { k_fwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
       } else {
-        const size_t sm = sizeof(V) * L.E;
+        const size_t sm = sizeof(T) == 4 ? 0 : sizeof(V) * L.E;
         auto kf = k_fwd_gemv_t<T>;
         MF_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
+        if (sizeof(T) == 4)
+          { k_pack_vec<<<cnt, 256, 0, ctx->stream>>>(M->tsave, M->tsave_off, nullptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
         dim3 g((unsigned)((L.B + 7) / 8), (unsigned)cnt);
-        { kf<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E); gbmhd::count_launch(); }
+        { kf<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
       }
     }
     MF_CUDA(cudaGetLastError());
@@ -1278,11 +1310,13 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       { k_bwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
       { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
     } else {
-      const size_t sm = sizeof(V) * L.n;
+      const size_t sm = sizeof(T) == 4 ? 0 : sizeof(V) * L.n;
       auto kb = k_bwd_gemv_t<T>;
-      MF_CUDA(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      MF_CUDA(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
+      if (sizeof(T) == 4)
+        { k_pack_vec<<<cnt, 256, 0, ctx->stream>>>(M->tsave, M->tsave_off, x, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
       dim3 g((unsigned)((L.E + 7) / 8), (unsigned)cnt);
-      { kb<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E); gbmhd::count_launch(); }
+      { kb<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
     }
     MF_CUDA(cudaGetLastError());
   }
