@@ -83,10 +83,11 @@ typedef struct {
 } gbmhd_params;
 
 /* Precision of the element matrices and of the preconditioner.
- *   GBMHD_FP64:        FP64 Jacobian (operator) and FP64 factors
- *   GBMHD_MIXED:       FP32 Jacobian (operator) and FP32 factors
- *   GBMHD_MIXED_F64OP: FP64 Jacobian (operator), FP32 factors
- * The residual, the Krylov vectors, Gram-Schmidt and the Newton update are FP64 in all. */
+ *   GBMHD_FP64:        FP64 Jacobian and FP64 factors
+ *   GBMHD_MIXED:       FP32 element matrices and FP32 factors (the preconditioner); the
+ *                      FGMRES operator is the FP64 Jacobian, the residual FP64
+ *   GBMHD_MIXED_F64OP: FP32 factors of the FP64 Jacobian; FP64 operator
+ * In every mode the residual, the Krylov vectors and the Newton update are FP64. */
 enum { GBMHD_FP64 = 0, GBMHD_MIXED = 1, GBMHD_MIXED_F64OP = 2 };
 
 /* Preconditioner of the FGMRES linear solve.
@@ -100,7 +101,7 @@ enum { GBMHD_FP64 = 0, GBMHD_MIXED = 1, GBMHD_MIXED_F64OP = 2 };
 enum { GBMHD_PC_MONOLITHIC = 0, GBMHD_PC_BADIA2024 = 1 };
 
 typedef struct {
-  int32_t precision;           /* GBMHD_FP64 or GBMHD_MIXED */
+  int32_t precision;           /* GBMHD_FP64, GBMHD_MIXED or GBMHD_MIXED_F64OP */
   int32_t max_newton;          /* Newton iteration cap (reference :niter) */
   double newton_rtol;          /* ‖r‖ ≤ max(atol, rtol‖r0‖) */
   double newton_atol;
