@@ -54,6 +54,7 @@ struct CellWork {
   T ph[NQ];
   T pp[NQ];
   T ugb[NQ][27];        // w det Σ_k u_k ∂_k N_b
+  T wn2[NQ][27];        // w det N_a
   T Bd[4][81];          // ∫ ψ_k div φ_(c,a)
   T Tm[4][81];          // Mp⁻¹ Bd
 };
@@ -326,46 +327,55 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
     for (int idx = tid; idx < NQ * 27; idx += nth) {
       const int q = idx / 27, b = idx % 27;
       w.ugb[q][b] = w.wdT[q] * (w.u[q][0] * w.G[q][0][b] + w.u[q][1] * w.G[q][1][b] + w.u[q][2] * w.G[q][2][b]);
+      w.wn2[q][b] = w.wdT[q] * tb.n2[q][b];
     }
     __syncthreads();
     const T beta = (T)P.beta, alpha = (T)P.alpha, gam = (T)P.gamma, sig = (T)P.sigma;
     const T zu = (T)P.zeta_u, zj = (T)P.zeta_j;
     const T B0 = (T)P.B[0], B1 = (T)P.B[1], B2 = (T)P.B[2];
-    // u-u: 27x27 scalar pairs, 9 component entries each.  K and the Picard part first,
-    // then the Newton part one test component at a time (3 accumulators live).
-    for (int idx = tid; idx < 27 * 27; idx += nth) {
-      const int a = idx / 27, b = idx % 27;
-      T K = 0, Cv = 0;
+    // u-u: 27x27 scalar pairs, 9 component entries each.  K = ∫ w ∇N_a·∇N_b and the Newton
+    // part M_cd = ∫ w N_a N_b ∂_d u_c are symmetric in (a, b), so each unordered pair a ≤ b
+    // (378 of them) forms them once and writes both (a, b) and (b, a); only the Picard part
+    // ∫ N_a (u·∇N_b) and the AL term are formed per ordered pair.
+    for (int idx = tid; idx < 27 * 28 / 2; idx += nth) {
+      int a = 0, r = idx;
+      while (r >= 27 - a) { r -= 27 - a; ++a; }
+      const int b = a + r;
+      T K = 0, Cab = 0, Cba = 0;
+      T Mg[9];  // Σ_q w N_a N_b ∂_d u_c at [d*3+c]
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Mg[k] = 0;
       for (int q = 0; q < NQ; ++q) {
         const T wd = w.wdT[q];
         K += wd * (w.G[q][0][a] * w.G[q][0][b] + w.G[q][1][a] * w.G[q][1][b] + w.G[q][2][a] * w.G[q][2][b]);
-        if (conv) Cv += tb.n2[q][a] * w.ugb[q][b];
-      }
-      const T diag = beta * K + alpha * Cv;
-      for (int c = 0; c < 3; ++c) {
-        T M0 = 0, M1 = 0, M2 = 0;
-        if (newton) {
-          for (int q = 0; q < NQ; ++q) {
-            const T m = w.wdT[q] * tb.n2[q][a] * tb.n2[q][b];
-            M0 += m * w.gu[q][0 * 3 + c];
-            M1 += m * w.gu[q][1 * 3 + c];
-            M2 += m * w.gu[q][2 * 3 + c];
-          }
+        if (conv) {
+          Cab += tb.n2[q][a] * w.ugb[q][b];
+          Cba += tb.n2[q][b] * w.ugb[q][a];
         }
-        const int ra = OU + c * 27 + a;
-        if (w.row[ra] < 0) continue;
-        const T Md[3] = {M0, M1, M2};
-        for (int d = 0; d < 3; ++d) {
-          const int cb = OU + d * 27 + b;
-          if (w.row[cb] < 0) continue;
-          T v = (c == d) ? diag : (T)0;
-          v += alpha * Md[d];
-          if (al_u) {
-            T s2 = 0;
-            for (int k = 0; k < 4; ++k) s2 += w.Bd[k][c * 27 + a] * w.Tm[k][d * 27 + b];
-            v += zu * s2;
+        if (newton) {
+          const T m = w.wn2[q][a] * tb.n2[q][b];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) Mg[k] += m * w.gu[q][k];
+        }
+      }
+      for (int side = 0; side < (a == b ? 1 : 2); ++side) {
+        const int ta = side ? b : a, tb_ = side ? a : b;  // test, trial
+        const T diag = beta * K + alpha * (side ? Cba : Cab);
+        for (int c = 0; c < 3; ++c) {
+          const int ra = OU + c * 27 + ta;
+          if (w.row[ra] < 0) continue;
+          for (int d = 0; d < 3; ++d) {
+            const int cb = OU + d * 27 + tb_;
+            if (w.row[cb] < 0) continue;
+            T v = (c == d) ? diag : (T)0;
+            v += alpha * Mg[d * 3 + c];
+            if (al_u) {
+              T s2 = 0;
+              for (int k = 0; k < 4; ++k) s2 += w.Bd[k][c * 27 + ta] * w.Tm[k][d * 27 + tb_];
+              v += zu * s2;
+            }
+            red_add(&val[w.rbase[ra] + ot[ra * ND + cb]], v);
           }
-          red_add(&val[w.rbase[ra] + ot[ra * ND + cb]], v);
         }
       }
     }
@@ -380,17 +390,17 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
         red_add(&val[w.rbase[rp] + ot[rp * ND + ru]], -s);
       }
     }
-    // u-j and j-u
+    // u-j and j-u: ∫ N_a (S_b × B) = (∫ N_a S_b) × B, the cross product after the sum
     for (int idx = tid; idx < 27 * 36; idx += nth) {
       const int a = idx / 36, b = idx % 36;
-      T c0 = 0, c1 = 0, c2 = 0;
+      T s0 = 0, s1 = 0, s2 = 0;
       for (int q = 0; q < NQ; ++q) {
-        const T m = w.wdT[q] * tb.n2[q][a];
-        const T s0 = w.S[q][0][b], s1 = w.S[q][1][b], s2 = w.S[q][2][b];
-        c0 += m * (s1 * B2 - s2 * B1);
-        c1 += m * (s2 * B0 - s0 * B2);
-        c2 += m * (s0 * B1 - s1 * B0);
+        const T m = w.wn2[q][a];
+        s0 += m * w.S[q][0][b];
+        s1 += m * w.S[q][1][b];
+        s2 += m * w.S[q][2][b];
       }
+      const T c0 = s1 * B2 - s2 * B1, c1 = s2 * B0 - s0 * B2, c2 = s0 * B1 - s1 * B0;
       const int rj = OJ + b;
       const T cc[3] = {c0, c1, c2};
 #pragma unroll
@@ -401,9 +411,11 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
         red_add(&val[w.rbase[rj] + ot[rj * ND + ru]], sig * cc[c]);
       }
     }
-    // j-j
-    for (int idx = tid; idx < 36 * 36; idx += nth) {
-      const int a = idx / 36, b = idx % 36;
+    // j-j: symmetric, one pass per unordered pair a ≤ b (666 of 36x36)
+    for (int idx = tid; idx < 36 * 37 / 2; idx += nth) {
+      int a = 0, r = idx;
+      while (r >= 36 - a) { r -= 36 - a; ++a; }
+      const int b = a + r;
       const int ra = OJ + a, rb = OJ + b;
       if (w.row[ra] < 0 || w.row[rb] < 0) continue;
       T s = 0;
@@ -413,6 +425,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
         s += w.wdT[q] * t;
       }
       red_add(&val[w.rbase[ra] + ot[ra * ND + rb]], s);
+      if (a != b) red_add(&val[w.rbase[rb] + ot[rb * ND + ra]], s);
     }
     // j-φ and φ-j
     for (int idx = tid; idx < 36 * 8; idx += nth) {

@@ -720,36 +720,49 @@ __device__ __forceinline__ void strided_dot_rows(SweepAcc<T> (&acc)[RowVec<T>::R
   }
 }
 
-// acc += Σ_{i<len} col[i] v[i] for one warp: lanes read 16-byte groups of four rows, sum the
-// products of four groups (16 terms) with FP32 FMAs (vector high and low parts separately)
-// and fold those short sums into the float-float accumulator.  col must be 16-byte aligned
-// and v zero-padded to a multiple of 4.
-__device__ __forceinline__ void warp_col_dot(SweepAcc<float>& acc, const float* __restrict__ col,
-                                             const float2* __restrict__ v, int len, int lane) {
+// acc[c] += Σ_{i<len} col0[c·ld + i] v[i], c < ncols ≤ NC, for one warp: each lane takes
+// 16-byte groups of four rows, loads the matching four packed vector entries once (two
+// 16-byte loads) and reuses them for the NC columns.  A lane sums the products of four
+// groups (16 terms per column) with FP32 FMAs, the vector's high and low parts separately,
+// and folds those short sums into the float-float accumulators.  col0 and ld·4 bytes must
+// be 16-byte aligned, v 16-byte aligned and zero-padded to a multiple of 4 entries.
+template <int NC>
+__device__ __forceinline__ void warp_cols_dot(SweepAcc<float> (&acc)[NC], const float* __restrict__ col0, int64_t ld,
+                                              int ncols, const float2* __restrict__ v, int len, int lane) {
   const int len4 = (len + 3) >> 2;
-  const float4* c4 = reinterpret_cast<const float4*>(col);
+  const float4* v4 = reinterpret_cast<const float4*>(v);  // two packed entries per float4
   for (int g0 = 0; g0 < len4; g0 += 128) {
-    float h = 0.0f, l = 0.0f;
+    float h[NC], l[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) h[c] = l[c] = 0.0f;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int g = g0 + lane + 32 * u;
       if (g < len4) {
-        const float4 m = __ldcs(c4 + g);
-        const float2 v0 = v[4 * g], v1 = v[4 * g + 1], v2 = v[4 * g + 2], v3 = v[4 * g + 3];
-        h = fmaf(m.x, v0.x, h); l = fmaf(m.x, v0.y, l);
-        h = fmaf(m.y, v1.x, h); l = fmaf(m.y, v1.y, l);
-        h = fmaf(m.z, v2.x, h); l = fmaf(m.z, v2.y, l);
-        h = fmaf(m.w, v3.x, h); l = fmaf(m.w, v3.y, l);
+        const float4 va = v4[2 * g], vb = v4[2 * g + 1];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          if (c < ncols) {  // warp-uniform
+            const float4 m = __ldcs(reinterpret_cast<const float4*>(col0 + c * ld) + g);
+            h[c] = fmaf(m.x, va.x, h[c]); l[c] = fmaf(m.x, va.y, l[c]);
+            h[c] = fmaf(m.y, va.z, h[c]); l[c] = fmaf(m.y, va.w, l[c]);
+            h[c] = fmaf(m.z, vb.x, h[c]); l[c] = fmaf(m.z, vb.y, l[c]);
+            h[c] = fmaf(m.w, vb.z, h[c]); l[c] = fmaf(m.w, vb.w, l[c]);
+          }
+        }
       }
     }
-    acc.merge(h, l);
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c].merge(h[c], l[c]);
   }
 }
 
-// Transposed sweeps (adjoint solves), one warp per column: each dot product runs down a
-// contiguous column of the column-major front.
+// Transposed sweeps (adjoint solves): a warp takes NC adjacent columns of a front and runs
+// down them together (each dot product is a contiguous column of the column-major front).
+// FP32 factors read the level's packed vector segments (vpk); FP64 factors stage theirs in
+// shared memory and use NC = 1.
 // forward, transposed: b[bnd_j] −= Σ_{i<ne} TR[i, j] t_i   (TR = rows 0..E of column E+j)
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) k_fwd_gemv_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
                                                     double* __restrict__ b, const double* __restrict__ tsave,
                                                     const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
@@ -767,22 +780,28 @@ __global__ void __launch_bounds__(256) k_fwd_gemv_t(const T* __restrict__ F, con
     __syncthreads();
   }
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int j = blockIdx.x * (blockDim.x / 32) + warp;
+  const int j = (blockIdx.x * (blockDim.x / 32) + warp) * NC;
   if (j >= nb) return;
+  const int ncols = min(NC, nb - j);
   const T* colj = F + f_off[f] + (int64_t)(E + j) * n;
-  SweepAcc<T> acc;
+  SweepAcc<T> acc[NC];
   if constexpr (sizeof(T) == 4) {
-    warp_col_dot(acc, colj, vpk + (int64_t)blockIdx.y * n, ne, lane);  // packed t of this front
+    warp_cols_dot<NC>(acc, colj, n, ncols, vpk + (int64_t)blockIdx.y * n, ne, lane);  // packed t of this front
   } else {
-    for (int i = lane; i < ne; i += 32) acc.add(colj[i], ts[i]);
+    static_assert(sizeof(T) == 4 || NC == 1, "FP64 transposed sweeps take one column per warp");
+    for (int i = lane; i < ne; i += 32) acc[0].add(colj[i], ts[i]);
   }
-  acc.warp_reduce();
-  if (lane == 0) atomicAdd(&b[bnd[bnd_ptr[f] + j]], -acc.value());
+  const int32_t* bd = bnd + bnd_ptr[f];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    acc[c].warp_reduce();
+    if (lane == 0 && c < ncols) atomicAdd(&b[bd[j + c]], -acc[c].value());
+  }
 }
 
 // backward, transposed: x[elim_i] = Σ_{c<ne} TL[c, i] t_c + Σ_{j<nb} BL[j, i] x_B[j]
 // (column i of the front: rows 0..E are TL, rows E.. are BL)
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256) k_bwd_gemv_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
                                                     double* __restrict__ x, const double* __restrict__ tsave,
                                                     const int64_t* __restrict__ toff, const int32_t* __restrict__ elim,
@@ -803,20 +822,26 @@ __global__ void __launch_bounds__(256) k_bwd_gemv_t(const T* __restrict__ F, con
     __syncthreads();
   }
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int i = blockIdx.x * (blockDim.x / 32) + warp;
+  const int i = (blockIdx.x * (blockDim.x / 32) + warp) * NC;
   if (i >= ne) return;
+  const int ncols = min(NC, ne - i);
   const T* coli = F + f_off[f] + (int64_t)i * n;
-  SweepAcc<T> acc;
+  SweepAcc<T> acc[NC];
   if constexpr (sizeof(T) == 4) {
     const float2* v = vpk + (int64_t)blockIdx.y * n;  // packed [t ; x_B] of this front
-    warp_col_dot(acc, coli, v, ne, lane);
-    warp_col_dot(acc, coli + E, v + E, nb, lane);
+    warp_cols_dot<NC>(acc, coli, n, ncols, v, ne, lane);
+    warp_cols_dot<NC>(acc, coli + E, n, ncols, v + E, nb, lane);
   } else {
-    for (int c = lane; c < ne; c += 32) acc.add(coli[c], vs[c]);
-    for (int j = lane; j < nb; j += 32) acc.add(coli[E + j], vs[E + j]);
+    static_assert(sizeof(T) == 4 || NC == 1, "FP64 transposed sweeps take one column per warp");
+    for (int c = lane; c < ne; c += 32) acc[0].add(coli[c], vs[c]);
+    for (int j = lane; j < nb; j += 32) acc[0].add(coli[E + j], vs[E + j]);
   }
-  acc.warp_reduce();
-  if (lane == 0) x[elim[elim_ptr[f] + i]] = acc.value();
+  const int32_t* el = elim + elim_ptr[f];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    acc[c].warp_reduce();
+    if (lane == 0 && c < ncols) x[el[i + c]] = acc[c].value();
+  }
 }
 
 // Packed (float-float) vector segments of a level's fronts for the transposed FP32 sweeps:
@@ -1376,6 +1401,18 @@ static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t
   return (int)std::max<int64_t>(64, std::min<int64_t>(cols, 1024));
 }
 
+// Columns per warp of the transposed FP32 sweeps: 4 while a level still gives at least two
+// 256-thread CTAs per SM, else fewer (levels with few, large fronts).  FP64 factors: 1.
+#define GT_NC(k) (sizeof(T) == 4 ? (k) : 1)
+template <typename T>
+static int gemv_t_cols(const gbmhd_ctx* ctx, int cols, int cnt) {
+  if (sizeof(T) != 4) return 1;
+  const int64_t want = 2LL * ctx->num_sms;
+  for (int nc = 4; nc > 1; nc /= 2)
+    if ((int64_t)cnt * ((cols + 8 * nc - 1) / (8 * nc)) >= want) return nc;
+  return 1;
+}
+
 template <typename T>
 static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool tr) {
   using V = typename SweepAcc<T>::V;
@@ -1400,11 +1437,12 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
         { k_fwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
       } else {
         const size_t sm = sizeof(T) == 4 ? 0 : sizeof(V) * L.E;
-        auto kf = k_fwd_gemv_t<T>;
+        const int nc = gemv_t_cols<T>(ctx, L.B, cnt);
+        auto kf = nc == 4 ? k_fwd_gemv_t<T, GT_NC(4)> : nc == 2 ? k_fwd_gemv_t<T, GT_NC(2)> : k_fwd_gemv_t<T, 1>;
         MF_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
         if (sizeof(T) == 4)
           { k_pack_vec<<<cnt, 256, 0, ctx->stream>>>(M->tsave, M->tsave_off, nullptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
-        dim3 g((unsigned)((L.B + 7) / 8), (unsigned)cnt);
+        dim3 g((unsigned)((L.B + 8 * nc - 1) / (8 * nc)), (unsigned)cnt);
         { kf<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
       }
     }
@@ -1429,11 +1467,12 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
     } else {
       const size_t sm = sizeof(T) == 4 ? 0 : sizeof(V) * L.n;
-      auto kb = k_bwd_gemv_t<T>;
+      const int nc = gemv_t_cols<T>(ctx, L.E, cnt);
+      auto kb = nc == 4 ? k_bwd_gemv_t<T, GT_NC(4)> : nc == 2 ? k_bwd_gemv_t<T, GT_NC(2)> : k_bwd_gemv_t<T, 1>;
       MF_CUDA(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
       if (sizeof(T) == 4)
         { k_pack_vec<<<cnt, 256, 0, ctx->stream>>>(M->tsave, M->tsave_off, x, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
-      dim3 g((unsigned)((L.E + 7) / 8), (unsigned)cnt);
+      dim3 g((unsigned)((L.E + 8 * nc - 1) / (8 * nc)), (unsigned)cnt);
       { kb<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
     }
     MF_CUDA(cudaGetLastError());
