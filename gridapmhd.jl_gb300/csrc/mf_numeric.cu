@@ -12,7 +12,12 @@ using namespace gbmhd;
 namespace {
 
 constexpr int NB = 64;   // Gauss-Jordan pivot block (inverted by one CTA)
-constexpr int PW = 128;  // panel: the trailing part of a front is updated once per PW pivots
+// panel: the trailing part of a front is updated once per PW pivots.  PW = 256 halves the
+// traffic again but multiplies the FP32 rounding of the panel's progressive inverse by the
+// conditioning of a 256-pivot block: at Ha = 500 (64x64x4) one solve in three then needed
+// 600+ FGMRES iterations instead of ~100.
+constexpr int PW = 128;
+static_assert(PW % NB == 0 && PW <= 256 && (PW & (PW - 1)) == 0, "k_panel_rows maps one thread per panel row");
 
 struct DevSym {
   int32_t* f_ne = nullptr;
@@ -436,7 +441,154 @@ __device__ __forceinline__ void df_rcp(float ah, float al, float& h, float& l) {
   l = __fsub_rn(d, __fsub_rn(h, x));
 }
 
-__global__ void __launch_bounds__(256) k_pivot_inverse_df(const float* __restrict__ F, int64_t off, int n, int k,
+// The 64x64 block lives in registers: thread (row ti = tid mod 64, column group tj = tid / 64,
+// CGN groups) holds the NB / CGN float-float entries A[ti, tj + CGN·u].  Per column step only
+// column c, the pivot row and the old row c pass through shared memory, with two barriers:
+//   (1) the two warps that hold column c copy it out and each reduces an argmax over its 32
+//       rows (high parts; ties: the lower row);
+//   (2) after the barrier: the pivot row's holders form the scaled pivot row r (r_c = 1 / pivot),
+//       row c's holders copy the old row c (it moves to row pr), and threads < 64 form the
+//       multipliers m_i = A[i, c] after the interchange;
+//   (3) after the barrier every thread updates its entries: row c becomes r, the others
+//       a − m_i r_j (column c: −m_i r_c).
+// The start of a step reads nothing that the previous step's (3) still needs, so the two
+// barriers per step suffice.  The chain of 64 steps is latency-bound: levels with few fronts
+// (one CTA per front) use CGN = 16 (1024 threads, 4 entries each) so that every SM
+// sub-partition has 8 warps to interleave; levels with many fronts use CGN = 4.
+__device__ __forceinline__ void df_sub_prod(float ah, float al, float m_h, float m_l, float r_h, float r_l, float& oh,
+                                            float& ol) {
+  // p = m · r in float-float
+  const float ph = __fmul_rn(m_h, r_h);
+  float pl = fmaf(m_h, r_h, -ph);
+  pl = fmaf(m_h, r_l, pl);
+  pl = fmaf(m_l, r_h, pl);
+  // a − p: TwoSum on the high parts, the low parts added to the error, renormalised by TwoSum
+  const float sh = __fsub_rn(ah, ph);
+  const float bv = __fsub_rn(sh, ah);
+  const float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(sh, bv)), __fsub_rn(-ph, bv));
+  const float sl = __fadd_rn(e, __fsub_rn(al, pl));
+  const float h = __fadd_rn(sh, sl);
+  const float hv = __fsub_rn(h, sh);
+  oh = h;
+  ol = __fadd_rn(__fsub_rn(sh, __fsub_rn(h, hv)), __fsub_rn(sl, hv));
+}
+
+template <int CGN>
+__global__ void __launch_bounds__(NB * CGN) k_pivot_inverse_df(const float* __restrict__ F, int64_t off, int n, int k,
+                                                              int kb, float* __restrict__ P, int32_t* err) {
+  static_assert(NB == 64 && NB % CGN == 0, "register layout: 64 rows x CGN column groups");
+  constexpr int NU = NB / CGN;
+  constexpr int LD = NB + 1;
+  __shared__ float Ob[NB * LD];  // the result, column-major, before the column interchanges
+  __shared__ float ch[NB], cl[NB], rh[NB], rl[NB], mh[NB], ml[NB], oh[NB], ol[NB];
+  __shared__ float cand_v[2];
+  __shared__ int cand_i[2];
+  __shared__ int perm[NB], colsrc[NB];
+  const int64_t f = blockIdx.x;
+  const float* M = F + off + f * (int64_t)n * n;
+  const int tid = threadIdx.x;
+  const int ti = tid & (NB - 1), tj = tid >> 6, lane = tid & 31;
+  float h[NU], l[NU];
+#pragma unroll
+  for (int u = 0; u < NU; ++u) {
+    const int j = tj + CGN * u;
+    h[u] = (ti < kb && j < kb) ? M[(k + ti) + (int64_t)(k + j) * n] : 0.0f;  // zero padding beyond kb
+    l[u] = 0.0f;
+  }
+  for (int c = 0; c < kb; ++c) {
+    const int uc = c / CGN;
+    // (1)
+    if (tj == c % CGN) {
+      float vh = 0.0f, vl = 0.0f;
+#pragma unroll
+      for (int u = 0; u < NU; ++u)
+        if (u == uc) { vh = h[u]; vl = l[u]; }
+      ch[ti] = vh;
+      cl[ti] = vl;
+      float best = (ti >= c && ti < kb) ? fabsf(vh) : -1.0f;
+      int bi = ti;
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (lane == 0) {
+        cand_v[ti >> 5] = best;
+        cand_i[ti >> 5] = bi;
+      }
+    }
+    __syncthreads();
+    // (2)
+    int pr = cand_i[0];
+    float pbest = cand_v[0];
+    if (cand_v[1] > pbest) { pbest = cand_v[1]; pr = cand_i[1]; }
+    if (!(pbest > 0.0f)) pr = c;  // singular block: keep going, the error flag is set below
+    if (ti == pr) {
+      float ih = 0.0f, il = 0.0f;
+      const float dh = ch[pr], dl = cl[pr];
+      if (dh != 0.0f) df_rcp(dh, dl, ih, il);
+#pragma unroll
+      for (int u = 0; u < NU; ++u) {
+        const int j = tj + CGN * u;
+        if (j == c) { rh[j] = ih; rl[j] = il; }
+        else df_mul(h[u], l[u], ih, il, rh[j], rl[j]);
+      }
+    }
+    if (ti == c) {
+#pragma unroll
+      for (int u = 0; u < NU; ++u) {
+        oh[tj + CGN * u] = h[u];
+        ol[tj + CGN * u] = l[u];
+      }
+    }
+    if (tid < NB) {
+      const int i = tid;
+      const int src = i == pr ? c : i;  // row i after the interchange holds the old row src
+      if (i == c) { mh[i] = 0.0f; ml[i] = 0.0f; }
+      else { mh[i] = ch[src]; ml[i] = cl[src]; }
+      if (i == 0) {
+        perm[c] = pr;
+        if (!(pbest > 0.0f)) atomicExch(err, 1);
+      }
+    }
+    __syncthreads();
+    // (3)
+    const float m_h = mh[ti], m_l = ml[ti];
+    const bool from_c = ti == pr && pr != c;  // this row now holds the old row c
+#pragma unroll
+    for (int u = 0; u < NU; ++u) {
+      const int j = tj + CGN * u;
+      const float r_h = rh[j], r_l = rl[j];
+      if (ti == c) {
+        h[u] = r_h;
+        l[u] = r_l;
+      } else {
+        float ah = from_c ? oh[j] : h[u], al = from_c ? ol[j] : l[u];
+        if (j == c) { ah = 0.0f; al = 0.0f; }
+        df_sub_prod(ah, al, m_h, m_l, r_h, r_l, h[u], l[u]);
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < NU; ++u) Ob[ti + (tj + CGN * u) * LD] = __fadd_rn(h[u], l[u]);
+  if (tid == 0) {  // undo the row interchanges as column interchanges, last first
+    for (int j = 0; j < kb; ++j) colsrc[j] = j;
+    for (int c = kb - 1; c >= 0; --c) {
+      const int p = perm[c];
+      const int t = colsrc[c];
+      colsrc[c] = colsrc[p];
+      colsrc[p] = t;
+    }
+  }
+  __syncthreads();
+  float* Pf = P + f * (int64_t)NB * NB;
+  for (int j = tj; j < NB; j += CGN)  // column-major, zero outside kb x kb
+    Pf[ti + j * NB] = (ti < kb && j < kb) ? Ob[ti + colsrc[j] * LD] : 0.0f;
+}
+
+// Shared-memory variant (block in shared memory, 6 CTAs per SM): levels with many fronts,
+// where the launch is throughput-bound rather than latency-bound.
+__global__ void __launch_bounds__(256) k_pivot_inverse_df_smem(const float* __restrict__ F, int64_t off, int n, int k,
                                                           int kb, float* __restrict__ P, int32_t* err) {
   // column-major with leading dimension LD = NB + 1: row accesses (swap, pivot row) are
   // free of bank conflicts
@@ -1283,7 +1435,12 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
       for (int k = p; k < p + pw; k += NB) {
         const int kb = std::min(NB, p + pw - k);
         if constexpr (sizeof(T) == 4)
-          { k_pivot_inverse_df<<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
+          {
+            if (cnt >= 2 * ctx->num_sms) k_pivot_inverse_df_smem<<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err);
+            else if (cnt >= ctx->num_sms) k_pivot_inverse_df<4><<<cnt, NB * 4, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err);
+            else k_pivot_inverse_df<16><<<cnt, NB * 16, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err);
+            gbmhd::count_launch();
+          }
         else
           { k_pivot_inverse<T><<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
         dim3 gc((unsigned)std::max(kb, (pw + 3) / 4), (unsigned)cnt);
