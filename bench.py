@@ -138,13 +138,20 @@ def compare_paths(args, ctx, mesh, dm, d_x_mixed, stream, opts):
     out = {}
     x_mixed = d_x_mixed.cpu().numpy()
     g = flow_rate(mesh, dm, 0.1)
+    ctx.sweep_stats()  # reset the sweep timers
     t = time.perf_counter()
     # λ to a relative residual of 1e-8 (the gradient target is 1e-6 relative)
     dJ, lam, arep, arc = ctx.adjoint(x_mixed, g, with_cells=True, precision=lib.GBMHD_MIXED, restart=200,
                                      max_linear=600, linear_rtol=1e-8)
     ta = time.perf_counter() - t
+    sw_n, sw_s, sw_bytes = ctx.sweep_stats()  # transposed preconditioner applications
     out["adjoint"] = {"seconds": ta, "rc": int(arc), "linear_iters": arep["linear_iters"],
-                      "time_setup_pc_s": arep["time_setup_pc_s"], "n_theta": int(len(dJ)),
+                      "time_setup_pc_s": arep["time_setup_pc_s"],
+                      "time_assembly_s": arep["time_assembly_s"], "time_linear_s": arep["time_linear_s"],
+                      "transposed_sweeps": {"applications": sw_n,
+                                            "ms_per_application": 1e3 * sw_s / sw_n if sw_n else None,
+                                            "achieved_gbs": sw_bytes * sw_n / sw_s / 1e9 if sw_s > 0 else None},
+                      "n_theta": int(len(dJ)),
                       "dJ_dgamma": float(dJ[0]), "dJ_dcw": float(dJ[1]),
                       "objective": "axial flow rate at z = 0.1",
                       "note": "host call (gbmhd_adjoint) at the mixed solution: FP64 transposed Jacobian, "
@@ -203,6 +210,8 @@ def run_ours(args):
         d_x.zero_()
         torch.cuda.synchronize()
         rep, rc = ctx.newton_solve_device(d_x.data_ptr(), **opts)
+        if rc != 0:
+            raise RuntimeError(f"Newton did not converge (warm-up): {rep}")
         reps.append(rep)
     torch.cuda.synchronize()
     L0 = lib.counters()
@@ -285,6 +294,7 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (Jacobian values alone 0.78 GB)"},
             "newton_solve_s": ms / 1e3, "newton_iters": last["newton_iters"], "linear_iters": last["linear_iters"],
             "linear_iters_per_step": [r["linear_iters"] for r in reps[-args.steps:]],
+            "pc_refactorizations": sum(r["pc_refactorizations"] for r in reps),
             "residual_history": [float("%.3e" % v) for v in last.get("residual_history", [])],
             "time_split_s": {k: last[k] for k in ("time_assembly_s", "time_setup_pc_s", "time_linear_s")},
             "assembly_cells_per_s": mesh.ncells / (asm_ms / 1e3), "jacobian_cells_per_s": mesh.ncells / (jac_ms / 1e3),

@@ -1139,18 +1139,24 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 
 // FWD: b[bnd_j] += Σ_{c<ne} M[E+j, c] t_c.   BWD: ybuf_i += Σ_v M[i, col(v)] w_v over v in this
 // CTA's chunk, w = [t ; −x_B], col(v) = v (v < ne) or E + (v − ne).
+//
+// The level's vector gather and scatter are folded in.  FWD reads t_c = b[elim_c] itself (the
+// level's eliminated dofs are not boundary dofs of any front of the level, so no CTA of the
+// launch writes them) and the CTAs of the first row tile save t for the backward sweep.  BWD
+// adds its partial sums straight into x[elim_i]; the solve zeroes x first.
 template <bool FWD>
 __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant__ CUtensorMap map, int64_t first,
                                                           int E, int rows, int cw, int chunks_a,
                                                           double* __restrict__ b,
-                                                          const double* __restrict__ x,
-                                                          const double* __restrict__ tsave,
+                                                          double* __restrict__ x,
+                                                          double* __restrict__ tsave,
                                                           const int64_t* __restrict__ toff,
                                                           const int32_t* __restrict__ bnd,
                                                           const int64_t* __restrict__ bnd_ptr,
+                                                          const int32_t* __restrict__ elim,
+                                                          const int64_t* __restrict__ elim_ptr,
                                                           const int32_t* __restrict__ f_ne,
-                                                          const int32_t* __restrict__ f_nb, double* __restrict__ ybuf,
-                                                          int32_t* err) {
+                                                          const int32_t* __restrict__ f_nb, int32_t* err) {
   extern __shared__ __align__(1024) unsigned char ts_raw[];
   float* tiles = reinterpret_cast<float*>(ts_raw);                  // [stage][column][row]
   float2* vs = reinterpret_cast<float2*>(ts_raw + (size_t)TS_STAGES * TS_COLS * rows * sizeof(float));  // [cw]
@@ -1161,10 +1167,15 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
   const int ne = f_ne[f], nb = f_nb[f];
   const int nrows = FWD ? nb : ne;
   const int row0 = blockIdx.x * rows;
-  if (row0 >= nrows) return;
   const bool seg_b = !FWD && (int)blockIdx.y >= chunks_a;
   const int c0 = (seg_b ? (int)blockIdx.y - chunks_a : (int)blockIdx.y) * cw;
   const int c1 = min(seg_b ? nb : ne, c0 + cw);
+  const int32_t* el = elim + elim_ptr[f];
+  if (FWD && blockIdx.x == 0) {  // save t for the backward sweep, also when the front has no rows here
+    double* ts = tsave + toff[f];
+    for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x) ts[c] = b[el[c]];
+  }
+  if (row0 >= nrows) return;
   if (c0 >= c1) return;
   const int ncol = c1 - c0;
   const int pcol0 = seg_b ? E + c0 : c0;
@@ -1185,7 +1196,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
   const double* t = tsave + toff[f];
   const int32_t* bd = bnd + bnd_ptr[f];
   for (int c = threadIdx.x; c < ncol; c += blockDim.x)
-    vs[c] = SweepAcc<float>::pack(seg_b ? -x[bd[c0 + c]] : t[c0 + c]);
+    vs[c] = SweepAcc<float>::pack(FWD ? b[el[c0 + c]] : seg_b ? -x[bd[c0 + c]] : t[c0 + c]);
   __syncthreads();
   SweepAcc<float> a0, a1;
   const int r = 2 * threadIdx.x;
@@ -1234,10 +1245,14 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
     if (i0 < nb) atomicAdd(&b[bd[i0]], a0.value());
     if (i0 + 1 < nb) atomicAdd(&b[bd[i0 + 1]], a1.value());
   } else {
-    double* y = ybuf + toff[f];
-    if (i0 < ne) atomicAdd(&y[i0], a0.value());
-    if (i0 + 1 < ne) atomicAdd(&y[i0 + 1], a1.value());
+    if (i0 < ne) atomicAdd(&x[el[i0]], a0.value());
+    if (i0 + 1 < ne) atomicAdd(&x[el[i0 + 1]], a1.value());
   }
+}
+
+__global__ void k_zero_at(const int32_t* __restrict__ idx, int64_t cnt, double* __restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x)
+    x[idx[i]] = 0.0;
 }
 
 __global__ void k_bwd_scatter(double* __restrict__ x, double* __restrict__ ybuf, const int64_t* __restrict__ toff,
@@ -1576,18 +1591,28 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
   const int rows_cta = SW_THREADS * RowVec<T>::R;
   const MFSymbolic& S = M->S;
   const T* F = reinterpret_cast<const T*>(M->F);
+  // the TMA backward sweeps add their partial sums into x directly: zero x at the dofs this
+  // factorization eliminates (the others, e.g. the p and φ blocks of the block-triangular
+  // preconditioner, hold the caller's values)
+  if (!tr && sizeof(T) == 4 && !S.elim.empty()) {
+    const int64_t ne_all = (int64_t)S.elim.size();
+    const unsigned gz = (unsigned)std::max<int64_t>(1, std::min<int64_t>((ne_all + 255) / 256, (int64_t)ctx->num_sms * 8));
+    { k_zero_at<<<gz, 256, 0, ctx->stream>>>(M->d.elim, ne_all, x); gbmhd::count_launch(); }
+  }
   for (size_t l = 0; l < S.levels.size(); ++l) {
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count;
-    { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first, L.E); gbmhd::count_launch(); }
+    const bool tma = !tr && sizeof(T) == 4 && M->map_ok[l];
+    if (!(tma && L.B > 0))  // the TMA forward sweep gathers t itself
+      { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first, L.E); gbmhd::count_launch(); }
     if (L.B > 0) {
-      if (!tr && sizeof(T) == 4 && M->map_ok[l]) {
+      if (tma) {
         const int rows = M->map_rows[2 * l];
         const int cw = tma_cols(ctx, L.B, rows, L.E, cnt);
         dim3 g((unsigned)((L.B + rows - 1) / rows), (unsigned)((L.E + cw - 1) / cw), (unsigned)cnt);
         const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
         MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        { k_sweep_tma<true><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l], L.first, L.E, rows, cw, 0, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, M->d_sweep_err); gbmhd::count_launch(); }
+        { k_sweep_tma<true><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l], L.first, L.E, rows, cw, 0, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.elim, M->d.elim_ptr, M->d.f_ne, M->d.f_nb, M->d_sweep_err); gbmhd::count_launch(); }
       } else if (!tr) {
         const int cols = sweep_cols(ctx, L.B, L.E, cnt, rows_cta);
         dim3 g((unsigned)((L.B + rows_cta - 1) / rows_cta), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
@@ -1615,8 +1640,7 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       dim3 g((unsigned)((L.E + rows - 1) / rows), (unsigned)(ca + cb), (unsigned)cnt);
       const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
       MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      { k_sweep_tma<false><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l + 1], L.first, L.E, rows, cw, ca, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, M->d_sweep_err); gbmhd::count_launch(); }
-      { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
+      { k_sweep_tma<false><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l + 1], L.first, L.E, rows, cw, ca, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.elim, M->d.elim_ptr, M->d.f_ne, M->d.f_nb, M->d_sweep_err); gbmhd::count_launch(); }
     } else if (!tr) {
       const int cols = sweep_cols(ctx, L.E, L.n, cnt, rows_cta);
       dim3 g((unsigned)((L.E + rows_cta - 1) / rows_cta), (unsigned)((L.n + cols - 1) / cols), (unsigned)cnt);

@@ -86,8 +86,19 @@ __global__ void k_spmv_f64(int64_t r0, int64_t n, const int64_t* __restrict__ ro
        row += ((int64_t)gridDim.x * blockDim.x) >> 3) {
     double acc = 0.0;
     if (row < n) {
+      // four nonzeros per lane in flight (column and value loads first, then the gathers);
+      // the matrix streams past L2 (evict-first), the vector stays resident
       const int64_t t1 = rowptr[row + 1];
-      for (int64_t t = rowptr[row] + sub; t < t1; t += 8) acc = fma(val[t], x[col[t]], acc);
+      int64_t t = rowptr[row] + sub;
+      for (; t + 24 < t1; t += 32) {
+        const int32_t c0 = __ldcs(col + t), c1 = __ldcs(col + t + 8), c2 = __ldcs(col + t + 16), c3 = __ldcs(col + t + 24);
+        const double v0 = __ldcs(val + t), v1 = __ldcs(val + t + 8), v2 = __ldcs(val + t + 16), v3 = __ldcs(val + t + 24);
+        acc = fma(v0, x[c0], acc);
+        acc = fma(v1, x[c1], acc);
+        acc = fma(v2, x[c2], acc);
+        acc = fma(v3, x[c3], acc);
+      }
+      for (; t < t1; t += 8) acc = fma(__ldcs(val + t), x[__ldcs(col + t)], acc);
     }
     for (int s = 4; s > 0; s >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s, 8);
     if (sub == 0 && row < n) y[row] = acc;
@@ -540,8 +551,12 @@ static int apply_pc(gbmhd_ctx* ctx, int precision, const double* v, double* z, b
 
 // FGMRES(m), right preconditioned, FP64 vectors.  Solves A x = b from x = 0.
 // Returns iterations in *iters; final relative residual in *rel.
+// With stagnated non-null, the solve also stops when the residual estimate is still above half
+// of |b| after kStagIters iterations (a preconditioner that does not work) and reports it there.
+constexpr int kStagIters = 100;
 static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int m, int maxit, double rtol,
-                  bool transpose, int* iters, double* rel, int verbose) {
+                  bool transpose, int* iters, double* rel, int verbose, bool* stagnated = nullptr) {
+  if (stagnated) *stagnated = false;
   Solver* s = ctx->solver;
   const int64_t n = ctx->ndofs;
   int rc = ensure_workspace(ctx, m);
@@ -604,6 +619,7 @@ static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int
       if (verbose > 1) std::fprintf(stderr, "  fgmres %d: %.3e\n", it, *rel);
       if (!std::isfinite(*rel)) { ctx->err = "FGMRES produced a non-finite residual"; return -3; }
       if (*rel <= rtol || hn == 0.0) { ++k; break; }
+      if (stagnated && it >= kStagIters && *rel > 0.5) { *stagnated = true; ++k; break; }
     }
     // x += Z y,  H y = g (upper triangular k x k)
     std::vector<double> y(k, 0.0);
@@ -615,7 +631,7 @@ static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int
     S_CUDA(cudaMemcpyAsync(s->hdev, y.data(), sizeof(double) * std::max(k, 1), cudaMemcpyHostToDevice, ctx->stream));
     { k_combine<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, k, s->Z, s->hdev, x); gbmhd::count_launch(); }
     S_CUDA(cudaGetLastError());
-    if (*rel <= rtol || it >= guard) break;
+    if (*rel <= rtol || it >= guard || (stagnated && *stagnated)) break;
     // restart: r = b − A x
     if ((rc = op(x, s->w))) return rc;
     { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, b, -1.0, s->w); gbmhd::count_launch(); }
@@ -734,10 +750,25 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     if ((rc = ensure_workspace(ctx, o->restart))) return rc;
     { k_scale_copy<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, -1.0, r, ctx->d_xtmp); gbmhd::count_launch(); }
     const double lin_rtol = std::min(o->linear_rtol, std::max(0.5 * target / rn, 1e-10));
+    bool stagnated = false;
     if ((rc = fgmres(ctx, GBMHD_FP64, ctx->d_xtmp, r, o->restart, o->max_linear, lin_rtol, false, &iters, &rel,
-                     o->verbose)))
+                     o->verbose, fprec == GBMHD_MIXED ? &stagnated : nullptr)))
       return rc;
     R.linear_iters += iters;
+    if (stagnated) {
+      // The FP32 factors carry the rounding of the FP32 assembly and extend-add (atomics in
+      // arbitrary order), so two factorizations of the same Jacobian differ; a rare one does
+      // not precondition at all.  Refactor once, in FP32 from the FP64 Jacobian at the current
+      // state, and solve the step again.
+      if (o->verbose) std::fprintf(stderr, "  linear solve stagnated (%d iterations, rel %.3e): refactoring\n", iters, rel);
+      R.pc_refactorizations += 1;
+      S_CUDA(cudaStreamSynchronize(ctx->stream));
+      if ((rc = setup_pc(ctx, fprec, o->preconditioner, &R.time_setup_pc_s))) return rc;
+      if ((rc = fgmres(ctx, GBMHD_FP64, ctx->d_xtmp, r, o->restart, o->max_linear, lin_rtol, false, &iters, &rel,
+                       o->verbose)))
+        return rc;
+      R.linear_iters += iters;
+    }
     { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, r, 1.0, d_x); gbmhd::count_launch(); }
     S_CUDA(cudaStreamSynchronize(ctx->stream));
     R.time_linear_s += now_s() - tl;

@@ -58,7 +58,7 @@ class Report(C.Structure):
                 ("initial_residual", C.c_double), ("final_residual", C.c_double),
                 ("time_assembly_s", C.c_double), ("time_setup_pc_s", C.c_double),
                 ("time_linear_s", C.c_double), ("time_total_s", C.c_double),
-                ("residual_history", C.c_double * 64)]
+                ("residual_history", C.c_double * 64), ("pc_refactorizations", C.c_int32)]
 
     def as_dict(self):
         n = min(self.newton_iters + 1, 64)
@@ -66,7 +66,8 @@ class Report(C.Structure):
                     converged=bool(self.converged), initial_residual=self.initial_residual,
                     final_residual=self.final_residual, time_assembly_s=self.time_assembly_s,
                     time_setup_pc_s=self.time_setup_pc_s, time_linear_s=self.time_linear_s,
-                    time_total_s=self.time_total_s, residual_history=list(self.residual_history[:n]))
+                    time_total_s=self.time_total_s, residual_history=list(self.residual_history[:n]),
+                    pc_refactorizations=self.pc_refactorizations)
 
 
 class Objective(C.Structure):

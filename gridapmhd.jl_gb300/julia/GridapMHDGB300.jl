@@ -64,7 +64,8 @@ mutable struct GbReport
   initial_residual::Float64; final_residual::Float64
   time_assembly_s::Float64; time_setup_pc_s::Float64; time_linear_s::Float64; time_total_s::Float64
   residual_history::NTuple{64,Float64}
-  GbReport() = new(0,0,0,0,0,0,0,0,0,ntuple(_->0.0,64))
+  pc_refactorizations::Int32
+  GbReport() = new(0,0,0,0,0,0,0,0,0,ntuple(_->0.0,64),0)
 end
 
 last_error(h) = unsafe_string(ccall((:gbmhd_last_error, LIB), Cstring, (Ptr{Cvoid},), h))

@@ -119,6 +119,8 @@ typedef struct {
   double initial_residual, final_residual;
   double time_assembly_s, time_setup_pc_s, time_linear_s, time_total_s;
   double residual_history[64]; /* ‖r‖ after each Newton step (first = initial) */
+  int32_t pc_refactorizations; /* mixed modes: FP32 factorizations redone after a linear solve
+                                  stagnated (0 in a normal solve) */
 } gbmhd_report;
 
 /* Objective J(x) of the adjoint: a linear functional of the free vector,
