@@ -33,6 +33,19 @@ struct RefTables {
   double frtg[6][NQF][36][3];     // reference gradient of that component
 };
 void build_ref_tables(RefTables& T);
+
+// Post-processing rule: degree 2(order+1) = 6, i.e. 4 Gauss-Legendre points per direction
+// (src/Applications/hunt.jl:247), with the bases the error integrals need.
+constexpr int NQP = 64;
+struct PostTables {
+  double w[NQP];                // weights on [0,1]^3
+  double q1[NQP][8];            // Q1 values (the geometry map)
+  double gq1[NQP][8][3];        // Q1 gradients
+  double n2[NQP][27];           // Q2 values
+  double g2[NQP][27][3];        // Q2 reference gradients
+  double rt[NQP][36];           // value of the single nonzero component of each RT function
+};
+void build_post_tables(PostTables& T);
 inline int rt_axis(int b) { return b / 12; }
 
 // Device-side float copy layouts are the same struct with float/double.
@@ -111,6 +124,7 @@ struct gbmhd_ctx {
   void* d_tab64 = nullptr;             // DevTables<double>
   void* d_tab32 = nullptr;             // DevTables<float>
   void* d_ftab = nullptr;              // FacetTables
+  void* d_posttab = nullptr;           // PostTables (built on first use)
   int64_t* d_rowptr = nullptr;
   int32_t* d_col = nullptr;
   int32_t* d_class = nullptr;

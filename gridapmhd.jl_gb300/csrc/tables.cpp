@@ -99,4 +99,33 @@ void build_ref_tables(RefTables& T) {
   }
 }
 
+void build_post_tables(PostTables& T) {
+  // 4-point Gauss-Legendre on [0,1]
+  const double t0 = 0.3399810435848562648, t1 = 0.8611363115940525752;
+  const double w0 = 0.6521451548625461427, w1 = 0.3478548451374538574;
+  const double gx[4] = {0.5 - 0.5 * t1, 0.5 - 0.5 * t0, 0.5 + 0.5 * t0, 0.5 + 0.5 * t1};
+  const double gw[4] = {0.5 * w1, 0.5 * w0, 0.5 * w0, 0.5 * w1};
+  std::memset(&T, 0, sizeof(T));
+  for (int k = 0; k < 4; ++k)
+    for (int j = 0; j < 4; ++j)
+      for (int i = 0; i < 4; ++i) {
+        const int q = i + 4 * j + 16 * k;
+        const double xi[3] = {gx[i], gx[j], gx[k]};
+        T.w[q] = gw[i] * gw[j] * gw[k];
+        for (int v = 0; v < 8; ++v) T.q1[q][v] = L1(v & 1, xi[0]) * L1((v >> 1) & 1, xi[1]) * L1((v >> 2) & 1, xi[2]);
+        q1_grads(xi, T.gq1[q]);
+        for (int n = 0; n < 27; ++n) {
+          const int a = n % 3, b = (n / 3) % 3, c = n / 9;
+          T.n2[q][n] = L2(a, xi[0]) * L2(b, xi[1]) * L2(c, xi[2]);
+          T.g2[q][n][0] = dL2(a, xi[0]) * L2(b, xi[1]) * L2(c, xi[2]);
+          T.g2[q][n][1] = L2(a, xi[0]) * dL2(b, xi[1]) * L2(c, xi[2]);
+          T.g2[q][n][2] = L2(a, xi[0]) * L2(b, xi[1]) * dL2(c, xi[2]);
+        }
+        for (int b = 0; b < 36; ++b) {
+          double div, g[3];
+          rt_eval(b, xi, T.rt[q][b], div, g);
+        }
+      }
+}
+
 }  // namespace gbmhd

@@ -23,7 +23,7 @@ GBMHD_PC_BADIA2024 = 1
 
 SYMBOLS = ["gbmhd_version", "gbmhd_create", "gbmhd_set_params", "gbmhd_sizes", "gbmhd_assemble",
            "gbmhd_assemble_device", "gbmhd_get_csr", "gbmhd_newton_solve", "gbmhd_newton_solve_device",
-           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_sweep_stats", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
+           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_sweep_stats", "gbmhd_hunt_errors", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -70,6 +70,15 @@ class Report(C.Structure):
                     pc_refactorizations=self.pc_refactorizations)
 
 
+class HuntAnalytic(C.Structure):
+    _fields_ = [("L", C.c_double), ("mu", C.c_double), ("grad_pz", C.c_double), ("sigma", C.c_double),
+                ("Ha", C.c_double), ("nsums", C.c_int32), ("u_scale", C.c_double), ("j_scale", C.c_double),
+                ("length_scale", C.c_double)]
+
+
+HUNT_NORMS = ("eu_h1", "eu_l2", "ej_l2", "eu_ref_h1", "eu_ref_l2", "ej_ref_l2", "uh_h1", "uh_l2", "jh_l2")
+
+
 class Objective(C.Structure):
     _fields_ = [("dJdx", _dp), ("n_theta_cells", C.c_int32)]
 
@@ -108,6 +117,7 @@ def load(path: Optional[str] = None):
     L.gbmhd_get_stream.restype = C.c_void_p
     L.gbmhd_diag_uj_solve_error.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, _dp]
     L.gbmhd_sweep_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), _dp, _dp]
+    L.gbmhd_hunt_errors.argtypes = [C.c_void_p, _dp, C.POINTER(HuntAnalytic), _dp]
     L.gbmhd_counters.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.gbmhd_destroy.argtypes = [C.c_void_p]
     L.gbmhd_destroy.restype = None
@@ -241,6 +251,18 @@ class Context:
         a, t, b = C.c_int64(), C.c_double(), C.c_double()
         self._check(self.L.gbmhd_sweep_stats(self.h, C.byref(a), C.byref(t), C.byref(b)), "gbmhd_sweep_stats")
         return a.value, t.value, b.value
+
+    def hunt_errors(self, x, *, L=1.0, mu=1.0, grad_pz=-1.0, sigma=1.0, Ha=10.0, nsums=10, u_scale=1.0,
+                    j_scale=1.0, length_scale=1.0):
+        """Norms of the hunt() post-processing (src/Applications/hunt.jl:238-260) on the device:
+        a dict with eu_h1, eu_l2, ej_l2, eu_ref_h1, eu_ref_l2, ej_ref_l2, uh_h1, uh_l2, jh_l2."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.shape != (self.ndofs,):
+            raise ValueError(f"x must have shape ({self.ndofs},)")
+        a = HuntAnalytic(L, mu, grad_pz, sigma, Ha, nsums, u_scale, j_scale, length_scale)
+        out = np.zeros(9)
+        self._check(self.L.gbmhd_hunt_errors(self.h, _ptr(x), C.byref(a), _ptr(out)), "gbmhd_hunt_errors")
+        return dict(zip(HUNT_NORMS, out.tolist()))
 
     def stream(self) -> int:
         return int(self.L.gbmhd_get_stream(self.h) or 0)

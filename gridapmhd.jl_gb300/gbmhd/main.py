@@ -328,6 +328,14 @@ def hunt(*, nc=(4, 4), ν=1.0, ρ=1.0, σ=1.0, B=(0.0, 10.0, 0.0), f=(0.0, 0.0, 
     for k, v in full["ptimer"].items():
         info[f"time_{k}"] = v
     dm = xh.dofmap
+    # post-processing (src/Applications/hunt.jl:211-260) on the device: the solved fields
+    # rescaled to physical units (uh = u0 ūh, jh = σ u0 B0 j̄h) against the analytic Hunt
+    # solution with nsums and 2·nsums Fourier terms, on the mesh warped by L
+    tpost = time.perf_counter()
+    norms = full["_context"].hunt_errors(xh.free_values, L=L, mu=ρ * ν, grad_pz=-float(f[2]) / ρ, sigma=σ,
+                                          Ha=Ha, nsums=nsums, u_scale=u0, j_scale=σ * u0 * B0, length_scale=L)
+    info.update(norms)
+    info["time_post_process"] = time.perf_counter() - tpost
     info.update(nc=list(nc), ncells=model.ncells, ndofs_u=dm.nfree["u"], ndofs_p=dm.nfree["p"],
                 ndofs_j=dm.nfree["j"], ndofs_φ=dm.nfree["phi"], ndofs=dm.ndofs, Re=Re, Ha=Ha, nsums=nsums,
                 kmap=[kmap_x, kmap_y], title=title)

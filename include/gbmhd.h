@@ -19,6 +19,9 @@
  *   gbmhd_param_gradient_noalloc  no counterpart in the reference (the adjoint's
  *                       parameter gradient from a given λ, without device allocation)
  *   gbmhd_get_csr       the assembled SparseMatrixCSR (pattern + values), for parity checks
+ *   gbmhd_hunt_errors   the post-processing of hunt(): error and solution norms against the
+ *                       analytic Hunt solution, src/Applications/hunt.jl:238-260 with
+ *                       analytical_hunt_u/j of :372-457
  *
  * Conventions
  *   - All host pointers are owned by the caller and only read during the call.
@@ -130,6 +133,19 @@ typedef struct {
   int32_t n_theta_cells;       /* >0: also return dJ/d f_z for every cell */
 } gbmhd_objective;
 
+/* Analytic Hunt solution for gbmhd_hunt_errors (src/Applications/hunt.jl:238-245). */
+typedef struct {
+  double L;                    /* half-width of the duct: a = b = L */
+  double mu;                   /* ρν */
+  double grad_pz;              /* −f_z/ρ */
+  double sigma;
+  double Ha;
+  int32_t nsums;               /* Fourier terms k = 0..nsums; the *_ref norms use k = 0..2·nsums */
+  double u_scale;              /* physical u = u_scale · the solved u (reference: u0) */
+  double j_scale;              /* physical j = j_scale · the solved j (reference: σ u0 B0) */
+  double length_scale;         /* physical x = length_scale · mesh x (reference: L, _warp at :352) */
+} gbmhd_hunt_analytic;
+
 int gbmhd_version(void);
 
 int gbmhd_create(gbmhd_ctx** out, const gbmhd_mesh* mesh, const gbmhd_dofmap* dofs,
@@ -195,6 +211,15 @@ void* gbmhd_get_stream(const gbmhd_ctx* ctx);
  * ‖x − A_uj⁻¹(A_uj x)‖/‖x‖ for a seeded random x, with the Jacobian assembled at the
  * device state d_state in the given precision. */
 int gbmhd_diag_uj_solve_error(gbmhd_ctx* ctx, const double* d_state, int32_t precision, double* err);
+
+/* Post-processing of hunt() (src/Applications/hunt.jl:238-260) on the device: with the
+ * free vector x_free (host) and the mesh's Dirichlet values, out[9] receives
+ *   {eu_h1, eu_l2, ej_l2, eu_ref_h1, eu_ref_l2, ej_ref_l2, uh_h1, uh_l2, jh_l2}
+ * where eu = u_analytic − u_h and ej = j_analytic − j_h with nsums (…_ref: 2·nsums) Fourier
+ * terms, integrated with 4 Gauss points per direction (degree 2(order+1) = 6). u_h and j_h
+ * are the solved fields times u_scale and j_scale; their values at the reference points
+ * of a cell do not change with length_scale, their gradients scale by 1/length_scale. */
+int gbmhd_hunt_errors(gbmhd_ctx* ctx, const double* x_free, const gbmhd_hunt_analytic* a, double* out);
 
 /* Diagnostics: multifrontal solves (preconditioner applications) timed with CUDA events
  * on the context stream since the last call, their total device time in seconds, and

@@ -266,3 +266,62 @@ def analytical_hunt_j(a, b, sigma, mu, grad_pz, Ha, n, x):
     out[:, 1] = a ** 2 * sigma ** 0.5 / mu ** 0.5 * (-grad_pz) * (-Hdx)
     out[(np.abs(xi) > 1) | (np.abs(eta) > 1)] = 0.0
     return out
+
+
+def analytical_hunt_grad_u(a, b, mu, grad_pz, Ha, n, x):
+    """∇ of analytical_hunt_u (src/Applications/hunt.jl:372-410) as [point][i][k] = ∂_i u_k: the
+    derivative of its Fourier series term by term (the reference differentiates the same
+    function with dual numbers when it forms ∇(u − uh), :250).  Only ∂_x u_z and ∂_y u_z are
+    nonzero."""
+    l = b / a
+    xi, eta = x[:, 0] / a, x[:, 1] / a
+    dxi = np.zeros(len(x)); deta = np.zeros(len(x))
+    for k in range(n + 1):
+        ak = (k + 0.5) * math.pi / l
+        N = math.sqrt(Ha ** 2 + 4 * ak ** 2)
+        r1, r2 = 0.5 * (Ha + N), 0.5 * (-Ha + N)
+        den1, den2 = 1 + math.exp(-2 * r1), 1 + math.exp(-2 * r2)
+        e11, e12 = np.exp(-r1 * (1 - eta)), np.exp(-r1 * (1 + eta))
+        e21, e22 = np.exp(-r2 * (1 - eta)), np.exp(-r2 * (1 + eta))
+        V2 = (r2 / N) * (e11 + e12) / den1
+        V3 = (r1 / N) * (e21 + e22) / den2
+        dV2 = (r2 / N) * r1 * (e11 - e12) / den1
+        dV3 = (r1 / N) * r2 * (e21 - e22) / den2
+        c = 2 * (-1) ** k / (l * ak ** 3)
+        dxi += -c * ak * np.sin(ak * xi) * (1 - V2 - V3)
+        deta += c * np.cos(ak * xi) * (-dV2 - dV3)
+    s = (-grad_pz) * a ** 2 / mu / a
+    out = np.zeros((len(x), 3, 3))
+    out[:, 0, 2] = s * dxi
+    out[:, 1, 2] = s * deta
+    out[(np.abs(xi) > 1) | (np.abs(eta) > 1)] = 0.0
+    return out
+
+
+def hunt_errors(cell_X, x_cell, L=1.0, mu=1.0, grad_pz=-1.0, sigma=1.0, Ha=10.0, nsums=10, u_scale=1.0,
+                j_scale=1.0, length_scale=1.0):
+    """The nine norms of hunt()'s post-processing (src/Applications/hunt.jl:238-260) with the
+    degree-6 rule (4 Gauss points per direction): eu_h1, eu_l2, ej_l2 (nsums terms), the
+    same with 2·nsums terms (…_ref), and uh_h1, uh_l2, jh_l2.  length_scale warps the mesh
+    (src/Applications/hunt.jl:352-357): points and measure scale, gradients of uh by 1/s."""
+    F = eval_fields(cell_X, x_cell, 4)
+    s = length_scale
+    xp = s * F[:, 0:3]
+    w = F[:, 3] * s ** 3
+    uh = u_scale * F[:, 4:7]
+    guh = u_scale * F[:, 7:16].reshape(-1, 3, 3) / s
+    jh = j_scale * F[:, 17:20]
+    out = {}
+    for tag, n in (("", nsums), ("_ref", 2 * nsums)):
+        ua = analytical_hunt_u(L, L, mu, grad_pz, Ha, n, xp)
+        gua = analytical_hunt_grad_u(L, L, mu, grad_pz, Ha, n, xp)
+        ja = analytical_hunt_j(L, L, sigma, mu, grad_pz, Ha, n, xp)
+        eu2 = np.sum((ua - uh) ** 2, 1)
+        ge2 = np.sum((gua - guh) ** 2, (1, 2))
+        out[f"eu{tag}_h1"] = math.sqrt(np.sum(w * (ge2 + eu2)))
+        out[f"eu{tag}_l2"] = math.sqrt(np.sum(w * eu2))
+        out[f"ej{tag}_l2"] = math.sqrt(np.sum(w * np.sum((ja - jh) ** 2, 1)))
+    out["uh_h1"] = math.sqrt(np.sum(w * (np.sum(uh * uh, 1) + np.sum(guh * guh, (1, 2)))))
+    out["uh_l2"] = math.sqrt(np.sum(w * np.sum(uh * uh, 1)))
+    out["jh_l2"] = math.sqrt(np.sum(w * np.sum(jh * jh, 1)))
+    return out
