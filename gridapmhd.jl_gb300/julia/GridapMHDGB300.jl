@@ -68,6 +68,11 @@ mutable struct GbReport
   GbReport() = new(0,0,0,0,0,0,0,0,0,ntuple(_->0.0,64),0)
 end
 
+struct GbHuntAnalytic
+  L::Float64; mu::Float64; grad_pz::Float64; sigma::Float64; Ha::Float64; nsums::Int32
+  u_scale::Float64; j_scale::Float64; length_scale::Float64
+end
+
 last_error(h) = unsafe_string(ccall((:gbmhd_last_error, LIB), Cstring, (Ptr{Cvoid},), h))
 check(rc, h, what) = rc < 0 ? error("$what failed ($rc): $(last_error(h))") : rc
 
@@ -125,6 +130,21 @@ end
 function gb300_postpro(cache, info)
   info[:nls_iters] = cache.report.newton_iters
   info[:ls_iters] = cache.report.linear_iters
+end
+
+# The norms of hunt()'s post-processing (src/Applications/hunt.jl:238-260) on the device,
+# for a hunt() driver that keeps the solver: pass the parameters hunt() derives there.
+function hunt_errors(nls::GB300NewtonSolver, x::AbstractVector; L, μ, grad_pz, σ, Ha, nsums, u0, B0)
+  a = GbHuntAnalytic(L, μ, grad_pz, σ, Ha, Int32(nsums), u0, σ * u0 * B0, L)
+  out = zeros(9)
+  xl = to_library_basis(nls, x)
+  GC.@preserve xl out begin
+    rc = ccall((:gbmhd_hunt_errors, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ref{GbHuntAnalytic}, Ptr{Float64}),
+               nls.handle[], xl, a, out)
+  end
+  check(rc, nls.handle[], "gbmhd_hunt_errors")
+  keys = (:eu_h1, :eu_l2, :ej_l2, :eu_ref_h1, :eu_ref_l2, :ej_ref_l2, :uh_h1, :uh_l2, :jh_l2)
+  Dict(zip(keys, out))
 end
 
 # ---------------------------------------------------------------- extraction
