@@ -759,15 +759,26 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
       // The FP32 factors carry the rounding of the FP32 assembly and extend-add (atomics in
       // arbitrary order), so two factorizations of the same Jacobian differ; a rare one does
       // not precondition at all.  Refactor once, in FP32 from the FP64 Jacobian at the current
-      // state, and solve the step again.
+      // state, and solve the step again; if that stagnates too, factor in FP64 (the plain
+      // path's preconditioner) for the rest of the solve.
       if (o->verbose) std::fprintf(stderr, "  linear solve stagnated (%d iterations, rel %.3e): refactoring\n", iters, rel);
       R.pc_refactorizations += 1;
       S_CUDA(cudaStreamSynchronize(ctx->stream));
       if ((rc = setup_pc(ctx, fprec, o->preconditioner, &R.time_setup_pc_s))) return rc;
       if ((rc = fgmres(ctx, GBMHD_FP64, ctx->d_xtmp, r, o->restart, o->max_linear, lin_rtol, false, &iters, &rel,
-                       o->verbose)))
+                       o->verbose, &stagnated)))
         return rc;
       R.linear_iters += iters;
+      if (stagnated) {
+        if (o->verbose) std::fprintf(stderr, "  stagnated again: FP64 factors\n");
+        R.pc_refactorizations += 1;
+        S_CUDA(cudaStreamSynchronize(ctx->stream));
+        if ((rc = setup_pc(ctx, GBMHD_FP64, o->preconditioner, &R.time_setup_pc_s))) return rc;
+        if ((rc = fgmres(ctx, GBMHD_FP64, ctx->d_xtmp, r, o->restart, o->max_linear, lin_rtol, false, &iters,
+                         &rel, o->verbose)))
+          return rc;
+        R.linear_iters += iters;
+      }
     }
     { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, r, 1.0, d_x); gbmhd::count_launch(); }
     S_CUDA(cudaStreamSynchronize(ctx->stream));
