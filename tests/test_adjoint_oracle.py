@@ -46,3 +46,34 @@ def test_oracle_adjoint_matches_finite_differences():
         fp[c, 2] *= 1 + h; fm[c, 2] *= 1 - h
         fd = (J_of(dict(params, f_cell=fp)) - J_of(dict(params, f_cell=fm))) / (2 * h * fcell[c, 2])
         assert abs(fd - dfz[c]) <= 1e-6 * abs(dfz).max(), (c, fd, dfz[c])
+
+
+def test_oracle_adjoint_pressure_drop_on_expansion():
+    """The inlet−outlet pressure drop of the sudden expansion (the second objective of the
+    adjoint) against central finite differences in γ and in the body force of one cell."""
+    from gbmhd.objectives import pressure_drop
+    from helpers import expansion_case
+    mesh, dm, params = expansion_case(Ha=8.0, Re=4.0)
+    fz = np.full(mesh.ncells, 0.5)
+    params["f_cell"] = np.stack([0 * fz, 0 * fz, fz], 1)
+    gauge = [dm.offsets["phi"]]
+    g = pressure_drop(mesh, dm)
+
+    def solve(p):
+        prob = oracle_problem(mesh, dm, p)
+        x, _ = O.newton_direct(prob, np.zeros(dm.ndofs), gauge=gauge, rtol=1e-14, maxiter=12)
+        return prob, x
+
+    prob, x = solve(params)
+    dgam, _, dfz, _ = oracle_adjoint(prob, dm, x, g, gauge)
+    h = 1e-6
+    Jp = g @ solve(dict(params, gamma=params["gamma"] * (1 + h)))[1]
+    Jm = g @ solve(dict(params, gamma=params["gamma"] * (1 - h)))[1]
+    fd = (Jp - Jm) / (2 * h * params["gamma"])
+    assert abs(fd - dgam) <= 1e-6 * abs(dgam), (fd, dgam)
+    c = mesh.ncells // 2
+    fp, fm = params["f_cell"].copy(), params["f_cell"].copy()
+    fp[c, 2] *= 1 + h
+    fm[c, 2] *= 1 - h
+    fd = (g @ solve(dict(params, f_cell=fp))[1] - g @ solve(dict(params, f_cell=fm))[1]) / (2 * h * fz[c])
+    assert abs(fd - dfz[c]) <= 1e-6 * abs(dfz).max(), (fd, dfz[c])
