@@ -130,6 +130,28 @@ def test_symbolic_structure(harness, mono):
     assert len(np.unique(S["ah_dst"])) == len(S["ah_dst"])
 
 
+@pytest.mark.parametrize("mono", [True, False])
+@pytest.mark.parametrize("case", [dict(nc=(6, 5), nz=3, Ha=10.0, Re=10.0, cw=0.01, Lz=0.2),
+                                  dict(nc=(16, 16), nz=4, Ha=500.0, Re=1.0, beta_map=3.0, cw=0.1, Lz=0.2)])
+def test_levels_keep_eliminated_and_boundary_dofs_apart(harness, mono, case):
+    """The TMA sweeps read b at a level's eliminated dofs while other CTAs of the same
+    launch add into b at the level's boundary dofs, and the backward sweep adds into x at
+    the eliminated dofs while reading x at the boundary ones.  Both need: no dof is
+    eliminated by one front of a level and a boundary dof of another front of that level,
+    and each front's eliminated and boundary dofs are distinct."""
+    mesh, dm, params = hunt_case(**case)
+    S = symbolic(harness, mesh, dm, mono)
+    for L in S["levels"]:
+        E, B, n, first, count = (int(v) for v in L[:5])
+        el = np.concatenate([S["elim"][S["elim_ptr"][f]:S["elim_ptr"][f + 1]] for f in range(first, first + count)])
+        bd = np.concatenate([S["bnd"][S["bnd_ptr"][f]:S["bnd_ptr"][f + 1]] for f in range(first, first + count)])
+        assert len(np.unique(el)) == len(el)
+        assert len(np.intersect1d(el, bd)) == 0
+        for f in range(first, first + count):
+            b = S["bnd"][S["bnd_ptr"][f]:S["bnd_ptr"][f + 1]]
+            assert len(np.unique(b)) == len(b)
+
+
 def test_emulated_factorization_solves_the_jacobian(harness):
     from oracle import oracle as O  # noqa: F401
     mesh, dm, params = hunt_case(nc=(6, 5), nz=3, Ha=10.0, Re=10.0, cw=0.01, Lz=0.2)
