@@ -650,8 +650,8 @@ void solver_destroy(gbmhd_ctx* ctx) {
   Solver* s = ctx->solver;
   if (!s) return;
   mf_destroy(s->mf);
-  void* ptrs[] = {s->Mp_inv, s->Mf_inv, s->seg, s->V, s->Z, s->w, s->t1, s->t2, s->x32, s->part, s->hdev,
-                  s->permT, s->valT};
+  void* ptrs[] = {s->reg, s->Mp_inv, s->Mf_inv, s->seg, s->V, s->Z, s->w, s->t1, s->t2, s->x32, s->part,
+                  s->hdev, s->permT, s->valT};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->hhost) cudaFreeHost(s->hhost);
