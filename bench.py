@@ -302,7 +302,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
             "gpu_launches": int(L1["launches"] - L0["launches"]),
             "library_gemm_calls": int(L1["gemm_calls"] - L0["gemm_calls"]),
-            "roofline": {"kernel": "multifrontal solve sweeps (k_fwd_chunk + k_bwd_chunk, one preconditioner "
+            "roofline": {"kernel": "multifrontal solve sweeps (k_sweep_tma<1> forward + k_sweep_tma<0> backward over all levels, one preconditioner "
                                    "application)", "bound": "hbm",
                          "achieved": sw_achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
                          "frac": sw_achieved / pk.get("hbm_gbs") if sw_achieved else None,
