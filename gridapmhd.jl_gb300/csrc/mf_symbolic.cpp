@@ -283,63 +283,67 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
     std::copy(t.elim.begin(), t.elim.end(), S.elim.begin() + S.elim_ptr[f]);
     std::copy(bnd[node_of[f]].begin(), bnd[node_of[f]].end(), S.bnd.begin() + S.bnd_ptr[f]);
   }
-  // arrowheads, level by level
-  std::vector<std::vector<int32_t>> lsrc(nlev);
-  std::vector<std::vector<int64_t>> ldst(nlev);
-  std::string err;
+  // arrowheads: the entries of each front's eliminated rows and of its boundary rows in the
+  // eliminated columns, front by front (fronts are numbered level by level, so each level's
+  // arrowheads are one contiguous range).  Two parallel passes over the fronts: count, then
+  // fill at the prefix-summed offsets; the result does not depend on the thread count.
+  auto front_arrowheads = [&](int64_t f, std::vector<int32_t>& pos, int32_t* src, int64_t* dst) -> int64_t {
+    const MFLevel& L = S.levels[S.f_level[f]];
+    const int32_t* el = S.elim.data() + S.elim_ptr[f];
+    const int32_t* bd = S.bnd.data() + S.bnd_ptr[f];
+    const int ne = S.f_ne[f], nb = S.f_nb[f];
+    for (int i = 0; i < ne; ++i) pos[el[i]] = i;
+    for (int i = 0; i < nb; ++i) pos[bd[i]] = L.E + i;
+    const int64_t base = S.f_off[f];
+    int64_t m = 0;
+    for (int i = 0; i < ne; ++i) {
+      const int32_t e = el[i];
+      for (int64_t t = rowptr[e]; t < rowptr[e + 1]; ++t) {
+        const int32_t k = col[t];
+        if (!is_uj[k] || pos[k] < 0) continue;
+        if (src) {
+          src[m] = (int32_t)t;
+          dst[m] = base + i + (int64_t)pos[k] * L.n;
+        }
+        ++m;
+      }
+    }
+    for (int i = 0; i < nb; ++i) {
+      const int32_t k = bd[i];
+      for (int64_t t = rowptr[k]; t < rowptr[k + 1]; ++t) {
+        const int32_t c = col[t];
+        if (!is_uj[c] || pos[c] < 0 || pos[c] >= L.E) continue;
+        if (src) {
+          src[m] = (int32_t)t;
+          dst[m] = base + (L.E + i) + (int64_t)pos[c] * L.n;
+        }
+        ++m;
+      }
+    }
+    for (int i = 0; i < ne; ++i) pos[el[i]] = -1;
+    for (int i = 0; i < nb; ++i) pos[bd[i]] = -1;
+    return m;
+  };
+  std::vector<int64_t> ah_off(nf + 1, 0);
 #pragma omp parallel
   {
     std::vector<int32_t> pos(ndofs, -1);
-    std::vector<int32_t> src;
-    std::vector<int64_t> dst;
-#pragma omp for schedule(dynamic, 1)
-    for (int32_t l = 0; l < nlev; ++l) {
-      src.clear();
-      dst.clear();
-      const MFLevel& L = S.levels[l];
-      for (int64_t f = L.first; f < L.first + L.count; ++f) {
-        const int32_t* el = S.elim.data() + S.elim_ptr[f];
-        const int32_t* bd = S.bnd.data() + S.bnd_ptr[f];
-        const int ne = S.f_ne[f], nb = S.f_nb[f];
-        for (int i = 0; i < ne; ++i) pos[el[i]] = i;
-        for (int i = 0; i < nb; ++i) pos[bd[i]] = L.E + i;
-        const int64_t base = S.f_off[f];
-        for (int i = 0; i < ne; ++i) {
-          const int32_t e = el[i];
-          for (int64_t t = rowptr[e]; t < rowptr[e + 1]; ++t) {
-            const int32_t k = col[t];
-            if (!is_uj[k] || pos[k] < 0) continue;
-            src.push_back((int32_t)t);
-            dst.push_back(base + i + (int64_t)pos[k] * L.n);
-          }
-        }
-        for (int i = 0; i < nb; ++i) {
-          const int32_t k = bd[i];
-          for (int64_t t = rowptr[k]; t < rowptr[k + 1]; ++t) {
-            const int32_t c = col[t];
-            if (!is_uj[c] || pos[c] < 0 || pos[c] >= L.E) continue;
-            src.push_back((int32_t)t);
-            dst.push_back(base + (L.E + i) + (int64_t)pos[c] * L.n);
-          }
-        }
-        for (int i = 0; i < ne; ++i) pos[el[i]] = -1;
-        for (int i = 0; i < nb; ++i) pos[bd[i]] = -1;
-      }
-      lsrc[l] = src;
-      ldst[l] = dst;
-    }
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t f = 0; f < nf; ++f) ah_off[f + 1] = front_arrowheads(f, pos, nullptr, nullptr);
   }
-  int64_t tot = 0;
-  for (int32_t l = 0; l < nlev; ++l) {
-    S.levels[l].ah_begin = tot;
-    tot += (int64_t)lsrc[l].size();
-    S.levels[l].ah_end = tot;
+  for (int64_t f = 0; f < nf; ++f) ah_off[f + 1] += ah_off[f];
+  S.ah_src.resize(ah_off[nf]);
+  S.ah_dst.resize(ah_off[nf]);
+#pragma omp parallel
+  {
+    std::vector<int32_t> pos(ndofs, -1);
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t f = 0; f < nf; ++f)
+      front_arrowheads(f, pos, S.ah_src.data() + ah_off[f], S.ah_dst.data() + ah_off[f]);
   }
-  S.ah_src.resize(tot);
-  S.ah_dst.resize(tot);
   for (int32_t l = 0; l < nlev; ++l) {
-    std::copy(lsrc[l].begin(), lsrc[l].end(), S.ah_src.begin() + S.levels[l].ah_begin);
-    std::copy(ldst[l].begin(), ldst[l].end(), S.ah_dst.begin() + S.levels[l].ah_begin);
+    S.levels[l].ah_begin = ah_off[S.levels[l].first];
+    S.levels[l].ah_end = ah_off[S.levels[l].first + S.levels[l].count];
   }
   // extend-add maps
   S.ea_ptr.assign(nf + 1, 0);
@@ -390,7 +394,7 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
       }
     }
   }
-  return err;
+  return "";
 }
 
 }  // namespace gbmhd

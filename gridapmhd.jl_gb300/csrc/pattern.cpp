@@ -62,24 +62,33 @@ std::string build_pattern(int64_t ncells, int64_t ndofs, const int32_t* cell_row
   }
   for (int64_t r = 0; r < ndofs; ++r)
     if (inc_ptr[r + 1] == inc_ptr[r]) return "a free dof belongs to no cell";
+  // the sorted distinct columns of row r: candidates from the row's cells, de-duplicated
+  // with a per-thread stamp array (one entry per dof) before the sort, so the sort sees
+  // each column once instead of once per cell that shares it
+  auto row_columns = [&](int64_t r, std::vector<int32_t>& stamp, std::vector<int32_t>& buf) {
+    buf.clear();
+    for (int64_t k = inc_ptr[r]; k < inc_ptr[r + 1]; ++k) {
+      const int64_t c = inc[k] / ND;
+      const int a = (int)(inc[k] % ND);
+      for (int b = 0; b < ND; ++b) {
+        const int32_t cb = cell_row[c * ND + b];
+        if (cb >= 0 && stamp[cb] != (int32_t)r && touched(a, b)) {
+          stamp[cb] = (int32_t)r;
+          buf.push_back(cb);
+        }
+      }
+    }
+    std::sort(buf.begin(), buf.end());
+  };
   // row lengths
   std::vector<int64_t> len(ndofs, 0);
 #pragma omp parallel
   {
-    std::vector<int32_t> buf;
+    std::vector<int32_t> buf, stamp(ndofs, -1);
 #pragma omp for schedule(dynamic, 1024)
     for (int64_t r = 0; r < ndofs; ++r) {
-      buf.clear();
-      for (int64_t k = inc_ptr[r]; k < inc_ptr[r + 1]; ++k) {
-        int64_t c = inc[k] / ND;
-        int a = (int)(inc[k] % ND);
-        for (int b = 0; b < ND; ++b) {
-          int32_t cb = cell_row[c * ND + b];
-          if (cb >= 0 && touched(a, b)) buf.push_back(cb);
-        }
-      }
-      std::sort(buf.begin(), buf.end());
-      len[r] = std::unique(buf.begin(), buf.end()) - buf.begin();
+      row_columns(r, stamp, buf);
+      len[r] = (int64_t)buf.size();
     }
   }
   P.rowptr.assign(ndofs + 1, 0);
@@ -90,37 +99,35 @@ std::string build_pattern(int64_t ncells, int64_t ndofs, const int32_t* cell_row
   P.col.resize(P.nnz);
 #pragma omp parallel
   {
-    std::vector<int32_t> buf;
+    std::vector<int32_t> buf, stamp(ndofs, -1);
 #pragma omp for schedule(dynamic, 1024)
     for (int64_t r = 0; r < ndofs; ++r) {
-      buf.clear();
-      for (int64_t k = inc_ptr[r]; k < inc_ptr[r + 1]; ++k) {
-        int64_t c = inc[k] / ND;
-        int a = (int)(inc[k] % ND);
-        for (int b = 0; b < ND; ++b) {
-          int32_t cb = cell_row[c * ND + b];
-          if (cb >= 0 && touched(a, b)) buf.push_back(cb);
-        }
-      }
-      std::sort(buf.begin(), buf.end());
-      auto e = std::unique(buf.begin(), buf.end());
-      std::copy(buf.begin(), e, P.col.begin() + P.rowptr[r]);
+      row_columns(r, stamp, buf);
+      std::copy(buf.begin(), buf.end(), P.col.begin() + P.rowptr[r]);
     }
   }
   // cell map with class de-duplication
   const size_t TS = (size_t)ND * ND;
+  // offsets of the cell's columns inside each of its rows: the cell's (column, slot) pairs
+  // are sorted once, then each row is walked once alongside them (a merge instead of a
+  // binary search per entry); entries of untouched blocks are 0xFFFF
   auto cell_table = [&](int64_t c, uint16_t* t) {
+    std::pair<int32_t, int> cb[ND];
+    int m = 0;
+    for (int b = 0; b < ND; ++b)
+      if (cell_row[c * ND + b] >= 0) cb[m++] = {cell_row[c * ND + b], b};
+    std::sort(cb, cb + m);
     for (int a = 0; a < ND; ++a) {
-      int32_t ra = cell_row[c * ND + a];
-      for (int b = 0; b < ND; ++b) {
-        int32_t rb = cell_row[c * ND + b];
-        uint16_t v = 0xFFFF;
-        if (ra >= 0 && rb >= 0 && touched(a, b)) {
-          const int32_t* beg = P.col.data() + P.rowptr[ra];
-          const int32_t* end = P.col.data() + P.rowptr[ra + 1];
-          v = (uint16_t)(std::lower_bound(beg, end, rb) - beg);
-        }
-        t[(size_t)a * ND + b] = v;
+      uint16_t* ta = t + (size_t)a * ND;
+      std::fill(ta, ta + ND, (uint16_t)0xFFFF);
+      const int32_t ra = cell_row[c * ND + a];
+      if (ra < 0) continue;
+      const int32_t* beg = P.col.data() + P.rowptr[ra];
+      const int32_t* end = P.col.data() + P.rowptr[ra + 1];
+      const int32_t* q = beg;
+      for (int i = 0; i < m; ++i) {
+        while (q < end && *q < cb[i].first) ++q;
+        if (touched(a, cb[i].second)) ta[cb[i].second] = (uint16_t)(q - beg);
       }
     }
   };
