@@ -22,7 +22,7 @@ import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-for p in (ROOT, os.path.join(ROOT, "gridapmhd.jl_gb300"), os.path.join(ROOT, "tests")):
+for p in (ROOT, os.path.join(ROOT, "gridapmhd.jl_gb300")):
     if p not in sys.path:
         sys.path.insert(0, p)
 
@@ -37,7 +37,7 @@ METRIC = "Newton-solve throughput (cells/s), Hunt 64x64x4 Ha=500, mixed precisio
 
 
 def workload(nc, nz, Lz, beta_map, Ha, Re, cw, tau, zeta, convection=2):
-    from helpers import hunt_case
+    from gbmhd.cases import hunt_case
     return hunt_case(nc=nc, nz=nz, Ha=Ha, Re=Re, beta_map=beta_map, Lz=Lz, cw=cw, tau=tau, zeta_u=zeta,
                      zeta_j=zeta, convection=convection)
 
@@ -90,11 +90,10 @@ def peaks():
 
 def cpu_sample(steps=1):
     """Oracle FP64 Newton (assembly + SuperLU) on the 12x12x4 sample of the same duct."""
-    from helpers import oracle_problem
     from oracle import oracle as O
     cfg = dict(CFG, nc=SAMPLE_NC, zeta=0.0)
     mesh, dm, params = workload(**cfg)
-    prob = oracle_problem(mesh, dm, params)
+    prob = O.problem_from_case(mesh, dm, params)
     times = []
     for _ in range(steps):
         t = time.perf_counter()
@@ -186,7 +185,7 @@ def compare_paths(args, ctx, mesh, dm, d_x_mixed, stream, opts):
 def run_ours(args):
     import torch
     from gbmhd import _build, lib
-    from helpers import gpu_context
+    from gbmhd.cases import gpu_context
     _build.build()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

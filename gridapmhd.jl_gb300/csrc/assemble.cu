@@ -745,6 +745,90 @@ __global__ void __launch_bounds__(128) k_param_derivs(int64_t ncells, const doub
   }
 }
 
+// ---------------------------------------------------------------------- dR/dα and dR/dβ
+// The residual of res_fluid_h1_hdiv (src/weakforms.jl:255-281) is linear in β (viscous term
+// ∫∇u⊙∇v, :264) and in α (convection ∫v·((∇u)ᵀ·u), :277-279, conv at :670), so on the u rows
+//   ∂R/∂β = ∫ Σ_i ∂_i u_c ∂_i N_n,   ∂R/∂α = ∫ N_n ((∇u)ᵀ·u)_c   (zero without convection).
+// In the MHD scaling (src/Applications/expansion.jl:113-123) Ha enters through α and β.
+// One CTA per cell: threads < 27 form the geometry and the state at their point; the 81 u
+// rows then sum over the points.
+__global__ void __launch_bounds__(128) k_param_derivs_ab(int64_t ncells, const double* __restrict__ cellX,
+                                                         const int32_t* __restrict__ gidx,
+                                                         const int32_t* __restrict__ row,
+                                                         const double* __restrict__ xfull,
+                                                         const DevTables<double>* __restrict__ tb,
+                                                         const GeoTables* __restrict__ geo, int convection,
+                                                         double* dr_dalpha, double* dr_dbeta) {
+  __shared__ double X[24], vu[81], wdet[NQ], Ji[NQ][9], gu[NQ][9], cv[NQ][3];
+  const int tid = threadIdx.x;
+  for (int64_t cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
+    __syncthreads();
+    if (tid < 24) X[tid] = cellX[cell * 24 + tid];
+    if (tid < 81) vu[tid] = xfull[gidx[cell * ND + OU + tid]];
+    __syncthreads();
+    if (tid < NQ) {
+      const int q = tid;
+      double J[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int a = 0; a < 3; ++a) {
+          double s = 0.0;
+          for (int v = 0; v < 8; ++v) s += X[3 * v + i] * geo->gq1[q][v][a];
+          J[i][a] = s;
+        }
+      const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      const double id = 1.0 / det;
+      double I[3][3];  // (J⁻¹)_{a i}
+      I[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * id;
+      I[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+      I[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+      I[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+      I[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+      I[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+      I[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * id;
+      I[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+      I[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+      wdet[q] = geo->w[q] * det;
+      for (int k = 0; k < 9; ++k) Ji[q][k] = I[k / 3][k % 3];
+      double u[3] = {0, 0, 0}, g[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // g[i][c] = ∂_i u_c
+      for (int n = 0; n < 27; ++n) {
+        double gn[3];
+        for (int i = 0; i < 3; ++i)
+          gn[i] = I[0][i] * tb->g2[q][n][0] + I[1][i] * tb->g2[q][n][1] + I[2][i] * tb->g2[q][n][2];
+        for (int c = 0; c < 3; ++c) {
+          const double val = vu[c * 27 + n];
+          u[c] += val * tb->n2[q][n];
+          for (int i = 0; i < 3; ++i) g[i][c] += val * gn[i];
+        }
+      }
+      for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) gu[q][i * 3 + c] = g[i][c];
+      for (int c = 0; c < 3; ++c) cv[q][c] = g[0][c] * u[0] + g[1][c] * u[1] + g[2][c] * u[2];
+    }
+    __syncthreads();
+    if (tid < 81) {
+      const int c = tid / 27, n = tid % 27;
+      double sb = 0.0, sa = 0.0;
+      for (int q = 0; q < NQ; ++q) {
+        double gd = 0.0;
+        for (int i = 0; i < 3; ++i) {
+          const double gn =
+              Ji[q][0 * 3 + i] * tb->g2[q][n][0] + Ji[q][1 * 3 + i] * tb->g2[q][n][1] + Ji[q][2 * 3 + i] * tb->g2[q][n][2];
+          gd += gu[q][i * 3 + c] * gn;
+        }
+        sb += wdet[q] * gd;
+        sa += wdet[q] * tb->n2[q][n] * cv[q][c];
+      }
+      const int32_t rr = row[cell * ND + tid];
+      if (rr >= 0) {
+        if (dr_dbeta) atomicAdd(&dr_dbeta[rr], sb);
+        if (dr_dalpha && convection != 0) atomicAdd(&dr_dalpha[rr], sa);
+      }
+    }
+  }
+}
+
 }  // namespace gbmhd
 
 using namespace gbmhd;
@@ -913,17 +997,26 @@ int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_
   return 0;
 }
 
-int gb_param_derivs(gbmhd_ctx* ctx, const double* d_x, double* d_dr_dgamma, double* d_dr_dcw, double* d_fz) {
+int gb_param_derivs(gbmhd_ctx* ctx, const double* d_x, double* d_dr_dgamma, double* d_dr_dcw, double* d_fz,
+                    double* d_dr_dalpha, double* d_dr_dbeta) {
   if (ctx->ndofs > 0)
     GB_CUDA(cudaMemcpyAsync(ctx->d_xfull, d_x, sizeof(double) * ctx->ndofs, cudaMemcpyDeviceToDevice,
                             ctx->stream));
   if (d_dr_dgamma) GB_CUDA(cudaMemsetAsync(d_dr_dgamma, 0, sizeof(double) * ctx->ndofs, ctx->stream));
   if (d_dr_dcw) GB_CUDA(cudaMemsetAsync(d_dr_dcw, 0, sizeof(double) * ctx->ndofs, ctx->stream));
+  if (d_dr_dalpha) GB_CUDA(cudaMemsetAsync(d_dr_dalpha, 0, sizeof(double) * ctx->ndofs, ctx->stream));
+  if (d_dr_dbeta) GB_CUDA(cudaMemsetAsync(d_dr_dbeta, 0, sizeof(double) * ctx->ndofs, ctx->stream));
   const GeoTables* geo = reinterpret_cast<const GeoTables*>(
       reinterpret_cast<const char*>(ctx->d_tab64) + ((sizeof(DevTables<double>) + 255) & ~size_t(255)));
   int64_t grid = ctx->num_sms * 8;
   if (grid > ctx->ncells) grid = ctx->ncells;
   if (grid < 1) grid = 1;
+  if (d_dr_dalpha || d_dr_dbeta) {
+    { k_param_derivs_ab<<<(unsigned)grid, 128, 0, ctx->stream>>>(
+        ctx->ncells, ctx->d_cellX, ctx->d_gidx, ctx->d_row, ctx->d_xfull,
+        reinterpret_cast<const DevTables<double>*>(ctx->d_tab64), geo, ctx->prm.convection, d_dr_dalpha, d_dr_dbeta); gbmhd::count_launch(); }
+    GB_CUDA(cudaGetLastError());
+  }
   { k_param_derivs<<<(unsigned)grid, 128, 0, ctx->stream>>>(
       ctx->ncells, ctx->d_cellX, ctx->d_gidx, ctx->d_row, reinterpret_cast<const unsigned long long*>(ctx->d_sign),
       ctx->d_xfull, reinterpret_cast<const DevTables<double>*>(ctx->d_tab64), geo, ctx->prm, d_dr_dgamma, d_fz); gbmhd::count_launch(); }

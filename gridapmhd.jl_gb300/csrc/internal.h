@@ -142,9 +142,10 @@ struct gbmhd_ctx {
 // assemble.cu
 int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_jac, int precision);
 int gb_upload_tables(gbmhd_ctx* ctx);
-// param derivatives used by the adjoint: dR/dγ, dR/dcw, f_z moments (all on device)
+// param derivatives used by the adjoint: dR/dγ, dR/dcw, f_z moments, dR/dα, dR/dβ (all on
+// device; a NULL output is skipped)
 int gb_param_derivs(gbmhd_ctx* ctx, const double* d_x, double* d_dr_dgamma, double* d_dr_dcw,
-                    double* d_fz /*[ncells][27]*/);
+                    double* d_fz /*[ncells][27]*/, double* d_dr_dalpha = nullptr, double* d_dr_dbeta = nullptr);
 
 #define GB_CUDA(call)                                                           \
   do {                                                                          \

@@ -76,6 +76,9 @@ int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, int values, const dou
 // b is overwritten in those entries.
 int mf_solve(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transpose);
 void mf_destroy(MFNumeric* M);
+// Waits for the context stream and returns -3 (with the message) if a solve sweep since the
+// last factorization gave up waiting for its TMA copies, 0 otherwise.
+int mf_check_sweeps(gbmhd_ctx* ctx, MFNumeric* M);
 // Solves timed since the last call (CUDA events on the context stream), their total
 // device time, and the factor bytes one solve reads; resets the counters.
 void mf_sweep_stats(MFNumeric* M, int64_t* applies, double* seconds, double* bytes_per_apply);

@@ -12,6 +12,7 @@ using namespace gbmhd;
 namespace {
 
 constexpr int NB = 64;   // Gauss-Jordan pivot block (inverted by one CTA)
+constexpr long kSweepWaitDefault = 1L << 22;  // spin limit of the sweeps' mbarrier waits
 // panel: the trailing part of a front is updated once per PW pivots.  PW = 256 halves the
 // traffic again but multiplies the FP32 rounding of the panel's progressive inverse by the
 // conditioning of a 256-pivot block: at Ha = 500 (64x64x4) one solve in three then needed
@@ -72,7 +73,8 @@ struct MFNumeric {
   void* d_sval = nullptr;           // scaled copy of the Jacobian values [nnz] (value precision)
   size_t sval_bytes = 0;
   int32_t* d_sweep_err = nullptr;   // set by a sweep whose TMA wait timed out
-  int32_t* h_sweep_err = nullptr;   // pinned copy, read at the next solve
+  int32_t* h_sweep_err = nullptr;   // pinned copy, read at the next solve and by mf_check_sweeps
+  long wait_limit = 0;              // spin limit of the sweeps' mbarrier waits
   // sweep timing: events around each solve, harvested when the next one starts
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ev_pending = false;
@@ -198,6 +200,8 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
   // non-finite FGMRES residual ends the solve), so the BF16x9 emulation need not scan its
   // operands for infinities and NaNs before every GEMM.
   MF_BLAS(cublasSetEmulationSpecialValuesSupport(M->blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE));
+  M->wait_limit = kSweepWaitDefault;
+  if (const char* wl = std::getenv("GBMHD_SWEEP_WAIT_LIMIT")) M->wait_limit = std::max(0L, std::atol(wl));
   const char* mode = std::getenv("GBMHD_FP32_GEMM");
   M->fp32_gemm_mode = (mode && std::strcmp(mode, "fp32") == 0) ? 1 : 0;
   return 0;
@@ -1102,7 +1106,7 @@ constexpr int TS_ROWS = 256;
 constexpr int TS_COLS = 16;
 constexpr int TS_STAGES = 4;
 constexpr int TS_THREADS = TS_ROWS / 2;   // launch bound; a level uses rows / 2 threads
-constexpr long TS_WAIT_LIMIT = 1L << 22;  // bounded mbarrier waits
+constexpr long TS_WAIT_LIMIT = kSweepWaitDefault;  // bounded mbarrier waits (default; GBMHD_SWEEP_WAIT_LIMIT)
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -1124,8 +1128,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
   return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase) {
-  for (long i = 0; i < TS_WAIT_LIMIT; ++i)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, long limit = TS_WAIT_LIMIT) {
+  for (long i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, phase)) return true;
   return false;
 }
@@ -1156,7 +1160,8 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
                                                           const int32_t* __restrict__ elim,
                                                           const int64_t* __restrict__ elim_ptr,
                                                           const int32_t* __restrict__ f_ne,
-                                                          const int32_t* __restrict__ f_nb, int32_t* err) {
+                                                          const int32_t* __restrict__ f_nb, int32_t* err,
+                                                          long wait_limit) {
   extern __shared__ __align__(1024) unsigned char ts_raw[];
   float* tiles = reinterpret_cast<float*>(ts_raw);                  // [stage][column][row]
   float2* vs = reinterpret_cast<float2*>(ts_raw + (size_t)TS_STAGES * TS_COLS * rows * sizeof(float));  // [cw]
@@ -1202,7 +1207,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
   const int r = 2 * threadIdx.x;
   for (int s = 0; s < nst; ++s) {
     const int buf = s % TS_STAGES;
-    if (mbar_wait_bounded(&full[buf], (uint32_t)(s / TS_STAGES) & 1u)) {
+    if (mbar_wait_bounded(&full[buf], (uint32_t)(s / TS_STAGES) & 1u, wait_limit)) {
       const float* tile = tiles + (size_t)buf * TS_COLS * rows;
       const float2* vv = vs + s * TS_COLS;
       const int cn = min(TS_COLS, ncol - s * TS_COLS);
@@ -1228,8 +1233,9 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
     __syncthreads();
     if (abort_flag) {
       if (threadIdx.x == 0) {  // let the copies in flight land before the CTA's shared memory is released
+        // (with the full limit, whatever limit the stage wait had)
         for (int s2 = s; s2 < min(nst, s + TS_STAGES); ++s2)
-          mbar_wait_bounded(&full[s2 % TS_STAGES], (uint32_t)(s2 / TS_STAGES) & 1u);
+          mbar_wait_bounded(&full[s2 % TS_STAGES], (uint32_t)(s2 / TS_STAGES) & 1u, TS_WAIT_LIMIT);
         atomicExch(err, 1);
       }
       return;
@@ -1552,6 +1558,10 @@ static int factor_scaled(gbmhd_ctx* ctx, MFNumeric* M, const V* val, const doubl
 
 int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, int values, const double* d_reg) {
   if (values == GBMHD_MIXED && !ctx->d_val32) { ctx->err = "multifrontal: no FP32 Jacobian assembled"; return -1; }
+  // new factors: a sweep timeout of an earlier solve no longer applies
+  MF_CUDA(cudaStreamSynchronize(ctx->stream));
+  MF_CUDA(cudaMemset(M->d_sweep_err, 0, sizeof(int32_t)));
+  *M->h_sweep_err = 0;
   if (values == GBMHD_FP64 && !ctx->d_val64) { ctx->err = "multifrontal: no FP64 Jacobian assembled"; return -1; }
   if (precision == GBMHD_MIXED) {
     if (values == GBMHD_MIXED) return factor_scaled<float, float>(ctx, M, ctx->d_val32, d_reg);
@@ -1612,7 +1622,7 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
         dim3 g((unsigned)((L.B + rows - 1) / rows), (unsigned)((L.E + cw - 1) / cw), (unsigned)cnt);
         const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
         MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        { k_sweep_tma<true><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l], L.first, L.E, rows, cw, 0, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.elim, M->d.elim_ptr, M->d.f_ne, M->d.f_nb, M->d_sweep_err); gbmhd::count_launch(); }
+        { k_sweep_tma<true><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l], L.first, L.E, rows, cw, 0, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.elim, M->d.elim_ptr, M->d.f_ne, M->d.f_nb, M->d_sweep_err, M->wait_limit); gbmhd::count_launch(); }
       } else if (!tr) {
         const int cols = sweep_cols(ctx, L.B, L.E, cnt, rows_cta);
         dim3 g((unsigned)((L.B + rows_cta - 1) / rows_cta), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
@@ -1640,7 +1650,7 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       dim3 g((unsigned)((L.E + rows - 1) / rows), (unsigned)(ca + cb), (unsigned)cnt);
       const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
       MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      { k_sweep_tma<false><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l + 1], L.first, L.E, rows, cw, ca, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.elim, M->d.elim_ptr, M->d.f_ne, M->d.f_nb, M->d_sweep_err); gbmhd::count_launch(); }
+      { k_sweep_tma<false><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l + 1], L.first, L.E, rows, cw, ca, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.elim, M->d.elim_ptr, M->d.f_ne, M->d.f_nb, M->d_sweep_err, M->wait_limit); gbmhd::count_launch(); }
     } else if (!tr) {
       const int cols = sweep_cols(ctx, L.E, L.n, cnt, rows_cta);
       dim3 g((unsigned)((L.E + rows_cta - 1) / rows_cta), (unsigned)((L.n + cols - 1) / cols), (unsigned)cnt);
@@ -1686,5 +1696,14 @@ int mf_solve(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transp
     M->ev_pending = true;
   }
   MF_CUDA(cudaMemcpyAsync(M->h_sweep_err, M->d_sweep_err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  return 0;
+}
+
+int mf_check_sweeps(gbmhd_ctx* ctx, MFNumeric* M) {
+  MF_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (*M->h_sweep_err) {
+    ctx->err = "multifrontal: a solve sweep's TMA wait timed out";
+    return -3;
+  }
   return 0;
 }

@@ -17,8 +17,10 @@
 // (two streams, or two contexts on one device) share the array and race.
 //
 // The device address of the array is looked up (cudaGetSymbolAddress) on the first call
-// made on a device, with that device current; make that first call before any stream
-// capture on the device.
+// made on a device, with that device current (the call checks that it is the context's
+// device); make that first call before any stream capture on the device.  The address is
+// cached per device for the life of the process: a cudaDeviceReset unloads the module and
+// invalidates it, so do not call this entry point after resetting a device.
 #include <mutex>
 
 #include "internal.h"
@@ -212,8 +214,16 @@ extern "C" int gbmhd_param_gradient_noalloc(gbmhd_ctx* ctx, const double* d_x, c
                std::to_string(kNoAllocMaxFacets);
     return -1;
   }
-  int dev = 0;
-  GB_CUDA(cudaGetDevice(&dev));
+  // The address is looked up with the context's device current: the kernels run on the
+  // context's stream, which belongs to that device.
+  int cur = 0;
+  GB_CUDA(cudaGetDevice(&cur));
+  if (cur != ctx->device) {
+    ctx->err = "param_gradient_noalloc: device " + std::to_string(cur) + " is current but the context lives on device " +
+               std::to_string(ctx->device) + "; make the context's device current first";
+    return -1;
+  }
+  const int dev = ctx->device;
   if (dev < 0 || dev >= kMaxDevices) { ctx->err = "param_gradient_noalloc: device id out of range"; return -1; }
   double* scratch = nullptr;
   {

@@ -554,6 +554,17 @@ static int apply_pc(gbmhd_ctx* ctx, int precision, const double* v, double* z, b
 // With stagnated non-null, the solve also stops when the residual estimate is still above half
 // of |b| after kStagIters iterations (a preconditioner that does not work) and reports it there.
 constexpr int kStagIters = 100;
+constexpr double kStagRel = 0.5;
+// Diagnostic overrides of the stagnation test (GBMHD_STAG_ITERS, GBMHD_STAG_REL), used by a
+// test that drives the refactorization and FP64-fallback path on purpose.
+static int stag_iters() {
+  const char* e = std::getenv("GBMHD_STAG_ITERS");
+  return e ? std::max(1, std::atoi(e)) : kStagIters;
+}
+static double stag_rel() {
+  const char* e = std::getenv("GBMHD_STAG_REL");
+  return e ? std::atof(e) : kStagRel;
+}
 static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int m, int maxit, double rtol,
                   bool transpose, int* iters, double* rel, int verbose, bool* stagnated = nullptr) {
   if (stagnated) *stagnated = false;
@@ -567,6 +578,8 @@ static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int
     return r;
   };
   S_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
+  const int s_iters = stag_iters();
+  const double s_rel = stag_rel();
   std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), h(m + 2);
   double bnorm = 0.0;
   if ((rc = dot(ctx, s, b, 1, b, &bnorm))) return rc;
@@ -619,7 +632,7 @@ static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int
       if (verbose > 1) std::fprintf(stderr, "  fgmres %d: %.3e\n", it, *rel);
       if (!std::isfinite(*rel)) { ctx->err = "FGMRES produced a non-finite residual"; return -3; }
       if (*rel <= rtol || hn == 0.0) { ++k; break; }
-      if (stagnated && it >= kStagIters && *rel > 0.5) { *stagnated = true; ++k; break; }
+      if (stagnated && it >= s_iters && *rel > s_rel) { *stagnated = true; ++k; break; }
     }
     // x += Z y,  H y = g (upper triangular k x k)
     std::vector<double> y(k, 0.0);
@@ -698,7 +711,9 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
   // GBMHD_MIXED_F64OP from the FP64 Jacobian.  (An FP32-Jacobian operator for the first
   // steps, i.e. Newton-level iterative refinement, measured 85–240 FGMRES iterations per
   // solve at Ha = 500 against 79–84 with the FP64 operator from the start.)
-  const int fprec = o->precision == GBMHD_FP64 ? GBMHD_FP64 : GBMHD_MIXED;
+  // precision of the factors: FP32 in the mixed modes until the stagnation safeguard moves
+  // it to FP64 for the rest of the solve
+  int fprec = o->precision == GBMHD_FP64 ? GBMHD_FP64 : GBMHD_MIXED;
   const bool fp32_elements = o->precision == GBMHD_MIXED;
   if (!ctx->d_val64) S_CUDA(cudaMalloc(&ctx->d_val64, sizeof(double) * ctx->nnz));
   if (fp32_elements && !ctx->d_val32) S_CUDA(cudaMalloc(&ctx->d_val32, sizeof(float) * ctx->nnz));
@@ -772,6 +787,7 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
       if (stagnated) {
         if (o->verbose) std::fprintf(stderr, "  stagnated again: FP64 factors\n");
         R.pc_refactorizations += 1;
+        fprec = GBMHD_FP64;  // the later steps keep the FP64 factors and skip the stagnation test
         S_CUDA(cudaStreamSynchronize(ctx->stream));
         if ((rc = setup_pc(ctx, GBMHD_FP64, o->preconditioner, &R.time_setup_pc_s))) return rc;
         if ((rc = fgmres(ctx, GBMHD_FP64, ctx->d_xtmp, r, o->restart, o->max_linear, lin_rtol, false, &iters,
@@ -780,6 +796,8 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
         R.linear_iters += iters;
       }
     }
+    // a preconditioner application whose TMA copies timed out was cut short: fail this step
+    if (ctx->solver->mf && (rc = mf_check_sweeps(ctx, ctx->solver->mf))) return rc;
     { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, r, 1.0, d_x); gbmhd::count_launch(); }
     S_CUDA(cudaStreamSynchronize(ctx->stream));
     R.time_linear_s += now_s() - tl;
@@ -842,7 +860,7 @@ extern "C" int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x, const gbmhd_object
   int rc = check_opts(ctx, o);
   if (rc) return rc;
   if (!x || !obj || !obj->dJdx || !dJ) { ctx->err = "adjoint: NULL argument"; return -1; }
-  const int64_t need = 2 + (obj->n_theta_cells > 0 ? ctx->ncells : 0);
+  const int64_t need = 4 + (obj->n_theta_cells > 0 ? ctx->ncells : 0);
   if (ntheta < need) { ctx->err = "adjoint: dJ_dtheta too short"; return -1; }
   if (!ctx->solver) ctx->solver = new Solver();
   if ((rc = ensure_workspace(ctx, o->restart))) return rc;
@@ -851,16 +869,17 @@ extern "C" int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x, const gbmhd_object
   gbmhd_report R{};
   const int64_t n = ctx->ndofs;
   double *d_x = nullptr, *d_g = nullptr, *d_lam = nullptr, *d_dg = nullptr, *d_dc = nullptr, *d_fz = nullptr,
-         *d_out = nullptr;
+         *d_out = nullptr, *d_da = nullptr, *d_db = nullptr;
   auto cleanup = [&]() {
-    for (double* p : {d_x, d_g, d_lam, d_dg, d_dc, d_fz, d_out})
+    for (double* p : {d_x, d_g, d_lam, d_dg, d_dc, d_fz, d_out, d_da, d_db})
       if (p) cudaFree(p);
   };
   auto fail = [&](int code) { cleanup(); return code; };
   if (cudaMalloc(&d_x, sizeof(double) * n) || cudaMalloc(&d_g, sizeof(double) * n) ||
       cudaMalloc(&d_lam, sizeof(double) * n) || cudaMalloc(&d_dg, sizeof(double) * n) ||
       cudaMalloc(&d_dc, sizeof(double) * n) || cudaMalloc(&d_fz, sizeof(double) * 27 * ctx->ncells) ||
-      cudaMalloc(&d_out, sizeof(double) * ctx->ncells)) {
+      cudaMalloc(&d_out, sizeof(double) * ctx->ncells) || cudaMalloc(&d_da, sizeof(double) * n) ||
+      cudaMalloc(&d_db, sizeof(double) * n)) {
     ctx->err = "adjoint: device allocation failed";
     return fail(-2);
   }
@@ -923,19 +942,21 @@ extern "C" int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x, const gbmhd_object
   }
   cudaFree(d_res);
   cudaFree(d_del);
+  if (s->mf && (rc = mf_check_sweeps(ctx, s->mf))) return fail(rc);
   R.linear_iters = total;
   R.final_residual = rel;
   R.time_linear_s = now_s() - tl;
-  if ((rc = gb_param_derivs(ctx, d_x, d_dg, d_dc, d_fz))) return fail(rc);
-  std::vector<double> tmp(2);
+  if ((rc = gb_param_derivs(ctx, d_x, d_dg, d_dc, d_fz, d_da, d_db))) return fail(rc);
+  std::vector<double> tmp(4);
   if ((rc = dot(ctx, s, d_lam, 1, d_dg, &tmp[0]))) return fail(rc);
   if ((rc = dot(ctx, s, d_lam, 1, d_dc, &tmp[1]))) return fail(rc);
-  dJ[0] = -tmp[0];
-  dJ[1] = -tmp[1];
+  if ((rc = dot(ctx, s, d_lam, 1, d_da, &tmp[2]))) return fail(rc);
+  if ((rc = dot(ctx, s, d_lam, 1, d_db, &tmp[3]))) return fail(rc);
+  for (int k = 0; k < 4; ++k) dJ[k] = -tmp[k];
   if (obj->n_theta_cells > 0) {
     { k_fz_grad<<<grid_for(ctx, ctx->ncells), 256, 0, ctx->stream>>>(ctx->ncells, ctx->d_row, d_lam, d_fz, d_out); gbmhd::count_launch(); }
     // the context stream is non-blocking: copy on it and wait for it
-    if (cudaMemcpyAsync(dJ + 2, d_out, sizeof(double) * ctx->ncells, cudaMemcpyDeviceToHost, ctx->stream) ||
+    if (cudaMemcpyAsync(dJ + 4, d_out, sizeof(double) * ctx->ncells, cudaMemcpyDeviceToHost, ctx->stream) ||
         cudaStreamSynchronize(ctx->stream)) {
       ctx->err = "adjoint: copy failed";
       return fail(-2);

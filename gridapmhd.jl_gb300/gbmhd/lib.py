@@ -231,7 +231,7 @@ class Context:
         x = np.ascontiguousarray(x, np.float64)
         g = np.ascontiguousarray(dJdx, np.float64)
         obj = Objective(_ptr(g), 1 if with_cells else 0)
-        nth = 2 + (self.ncells if with_cells else 0)
+        nth = 4 + (self.ncells if with_cells else 0)
         out = np.zeros(nth)
         lam = np.zeros(self.ndofs)
         o = make_opts(**opts)

@@ -89,3 +89,18 @@ def pressure_drop(mesh: StructuredMesh, dm: DofMap, inlet_tag="inlet", outlet_ta
             rows = gd[cells, OP + k]
             np.add.at(g, rows, sign * mom[:, k] / V)
     return g
+
+
+def ha_gradient(dJ: np.ndarray, Ha: float, Re: float, scaling: str = "cfd") -> float:
+    """dJ/dHa from gbmhd_adjoint's parameter gradient dJ = [dJ/dγ, dJ/dcw, dJ/dα, dJ/dβ, ...].
+
+    * ``"cfd"`` scaling (src/Applications/hunt.jl:125-128): α = 1, β = 1/Re, γ = N = Ha²/Re,
+      so dJ/dHa = dJ/dγ · 2Ha/Re.
+    * ``"mhd"`` scaling (src/Applications/expansion.jl:113-123): α = 1/N = Re/Ha², β = 1/Ha²,
+      γ = 1, so dJ/dHa = −(2/Ha³)(Re·dJ/dα + dJ/dβ).
+    """
+    if scaling == "cfd":
+        return float(dJ[0]) * 2.0 * Ha / Re
+    if scaling == "mhd":
+        return -2.0 / Ha ** 3 * (Re * float(dJ[2]) + float(dJ[3]))
+    raise ValueError(f"unknown scaling {scaling!r}: expected 'cfd' or 'mhd'")

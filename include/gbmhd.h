@@ -181,8 +181,11 @@ int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x_inout, const gbmhd_sol
 
 /* Discrete adjoint at a converged state x (host [ndofs]): solves Jᵀλ = ∂J/∂x and
  * returns dJ/dθ = −λᵀ ∂R/∂θ in dJ_dtheta: [0] d/dγ, [1] d/d(cw) (all thin-wall
- * facets together), [2 .. 2+ncells) d/d f_z per cell (when n_theta_cells > 0).
- * lambda_out (host [ndofs]) may be NULL. */
+ * facets together), [2] d/dα, [3] d/dβ, [4 .. 4+ncells) d/d f_z per cell (when
+ * n_theta_cells > 0; ntheta must then be ≥ 4 + ncells, else ≥ 4).  Ha enters through
+ * γ = Ha²/Re in the CFD scaling (src/Applications/hunt.jl:125-128) and through α = Re/Ha²,
+ * β = 1/Ha² in the MHD scaling (src/Applications/expansion.jl:113-123); the host applies
+ * the chain rule.  lambda_out (host [ndofs]) may be NULL. */
 int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x_free, const gbmhd_objective* obj,
                   const gbmhd_solve_opts* opts, double* dJ_dtheta, int64_t ntheta, double* lambda_out,
                   gbmhd_report* report);
@@ -200,7 +203,10 @@ int gbmhd_adjoint(gbmhd_ctx* ctx, const double* x_free, const gbmhd_objective* o
  * needs zeroing.  The scratch is shared by every context on a device: calls that
  * overlap on the GPU (several streams or host threads) race.  The first call on a
  * device looks up the array's address with that device current; make it before any
- * stream capture. */
+ * stream capture.  The context's device must be the current device (else -1).  The
+ * address stays cached until the process exits, so a cudaDeviceReset invalidates it.
+ * In the MHD scaling (α = 1/N, β = 1/Ha²) Ha does not enter through γ: there dJ/dγ is
+ * not dJ/dHa, and gbmhd_adjoint's dJ/dα and dJ/dβ are needed for it. */
 int gbmhd_param_gradient_noalloc(gbmhd_ctx* ctx, const double* d_x, const double* d_lambda, double* d_out);
 
 /* The CUDA stream (cudaStream_t) every call on this context is issued on; a
@@ -225,6 +231,21 @@ int gbmhd_hunt_errors(gbmhd_ctx* ctx, const double* x_free, const gbmhd_hunt_ana
  * on the context stream since the last call, their total device time in seconds, and
  * the factor bytes one solve reads (padding excluded); resets the counters. */
 int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double* bytes_per_apply);
+
+/* Diagnostic environment variables.  None is needed in normal use; without them the
+ * library's behaviour is fixed.  They exist for measurements and for tests that drive
+ * rarely taken paths on purpose.
+ *   GBMHD_PC_EPS32, GBMHD_PC_EPS64  scale of the root's −ε·diag(mass) regularisation of the
+ *                                   global p and φ pivots (FP32 / FP64 factors; default 1)
+ *   GBMHD_ELIM_ORDER                field order of elimination inside a front (default "jufp")
+ *   GBMHD_STAG_ITERS, GBMHD_STAG_REL  the mixed-precision stagnation test: a linear solve
+ *                                   that has run GBMHD_STAG_ITERS iterations (default 100) with
+ *                                   its relative residual still above GBMHD_STAG_REL (default
+ *                                   0.5) triggers the refactorization / FP64 fallback
+ *   GBMHD_SWEEP_WAIT_LIMIT          spin limit of the TMA solve sweeps' mbarrier waits, read
+ *                                   when a context first factors (default 4,194,304); a wait
+ *                                   that runs out drains its copies and makes the Newton step
+ *                                   or the adjoint return -3 */
 
 /* Diagnostics: kernels launched by this library and cuBLAS GEMM calls it made
  * since it was loaded (all contexts together). */

@@ -572,6 +572,51 @@ void orc_param_derivs(int64_t ncells, const double* cell_X, const double* x_cell
   }
 }
 
+// ∂R/∂β and ∂R/∂α on the u rows (the residual is linear in both): the viscous term
+// ∫∇u⊙∇v and the convection term ∫v·((∇u)ᵀ·u) of res_fluid_h1_hdiv
+// (src/weakforms.jl:264, :277-279; conv at :670).  The convection derivative is zero for
+// convection = :none.  In the MHD scaling (src/Applications/expansion.jl:113-123) Ha enters
+// through α = 1/N = Re/Ha² and β = 1/Ha², so dJ/dHa needs these two.
+void orc_param_derivs_ab(int64_t ncells, const double* cell_X, const double* x_cell, const OrcFluid* fl,
+                         double* dr_dalpha /*[ncells][129]*/, double* dr_dbeta /*[ncells][129]*/) {
+  double gx[3], gw[3];
+  gauss_legendre01(3, gx, gw);
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < ncells; ++c) {
+    const double* X = cell_X + 24 * c;
+    const double* xl = x_cell + ND * c;
+    std::memset(dr_dalpha + ND * c, 0, sizeof(double) * ND);
+    std::memset(dr_dbeta + ND * c, 0, sizeof(double) * ND);
+    for (int qk = 0; qk < 3; ++qk)
+      for (int qj = 0; qj < 3; ++qj)
+        for (int qi = 0; qi < 3; ++qi) {
+          double xi[3] = {gx[qi], gx[qj], gx[qk]};
+          PhysBasis P;
+          eval_phys(X, xi, P);
+          const double w = gw[qi] * gw[qj] * gw[qk] * P.det;
+          double u[3] = {0, 0, 0}, gu[3][3] = {{0}};  // gu[i][k] = ∂_i u_k
+          for (int cc = 0; cc < 3; ++cc)
+            for (int n = 0; n < 27; ++n) {
+              const double val = xl[OU + cc * 27 + n];
+              u[cc] += val * P.u[n];
+              for (int i = 0; i < 3; ++i) gu[i][cc] += val * P.gu[n][i];
+            }
+          double conv[3];  // (∇u)ᵀ·u
+          for (int cc = 0; cc < 3; ++cc) {
+            conv[cc] = 0.0;
+            for (int k = 0; k < 3; ++k) conv[cc] += gu[k][cc] * u[k];
+          }
+          for (int cc = 0; cc < 3; ++cc)
+            for (int n = 0; n < 27; ++n) {
+              double g = 0.0;
+              for (int i = 0; i < 3; ++i) g += gu[i][cc] * P.gu[n][i];
+              dr_dbeta[ND * c + OU + cc * 27 + n] += w * g;
+              if (fl->convection != 0) dr_dalpha[ND * c + OU + cc * 27 + n] += w * P.u[n] * conv[cc];
+            }
+        }
+  }
+}
+
 // Field evaluation for post-processing: at every cell, `npts1d`^3 Gauss points,
 // write the physical point, weight·det J, u, ∇u (9, [i][k] = ∂_i u_k), p, j, div j, φ.
 // out layout per point: 3 + 1 + 3 + 9 + 1 + 3 + 1 + 1 = 22 doubles.

@@ -45,6 +45,7 @@ def lib():
         _LIB = C.CDLL(path)
         _LIB.orc_assemble_cells.restype = None
         _LIB.orc_param_derivs.restype = None
+        _LIB.orc_param_derivs_ab.restype = None
         _LIB.orc_eval_fields.restype = None
     return _LIB
 
@@ -177,6 +178,19 @@ class OracleProblem:
         return r, A
 
 
+def problem_from_case(mesh, dm, params) -> OracleProblem:
+    """The oracle's problem for a (mesh, dof map, parameters) workload of the host mirror
+    (gbmhd.cases): the same cells, dof numbering, Dirichlet values and physical parameters."""
+    fl = Fluid(alpha=params["alpha"], beta=params["beta"], gamma=params["gamma"], sigma=params["sigma"],
+               B=params["B"], f=params["f"], zeta_u=params["zeta_u"], zeta_j=params["zeta_j"],
+               convection=params["convection"], f_cell=params.get("f_cell"))
+    fc = None
+    if params.get("facets") is not None:
+        q = params["facets"]
+        fc = Facets(cell=q["cell"], lface=q["lface"], tau=q["tau"], cw=q["cw"], jw=q["jw"], phi0=q.get("phi0"))
+    return OracleProblem(mesh.cell_coords(), dm.global_cell_dofs(), dm.ndofs, dm.cell_values, fl, fc)
+
+
 def newton_direct(prob: OracleProblem, x0, gauge: Sequence[int] = (), rtol=1e-10, atol=0.0, maxiter=10,
                   verbose=False):
     """Newton with a sparse direct solve (SuperLU), dropping the gauge dofs."""
@@ -201,6 +215,36 @@ def newton_direct(prob: OracleProblem, x0, gauge: Sequence[int] = (), rtol=1e-10
         if verbose:
             print(f"newton {it}: |r| = {hist[-1]:.3e}")
         if hist[-1] <= max(atol, rtol * r0):
+            break
+    return x, dict(nls_iters=it, residuals=hist)
+
+
+def newton_chord(prob: OracleProblem, x0, gauge: Sequence[int] = (), rtol=1e-13, atol=0.0, maxiter=60,
+                 verbose=False):
+    """Newton's root with one SuperLU factorization (the chord method).
+
+    The residual is evaluated exactly at every step (FP64 assembly); only the Jacobian is
+    frozen at x0.  The iteration therefore converges to the same root as the Newton
+    iteration of the :julia solver (src/main.jl:181-186), only more slowly.  This is
+    for meshes where SuperLU takes minutes per factorization (the 32x32x3 duct)."""
+    x = np.array(x0, dtype=float, copy=True)
+    keep = np.ones(prob.ndofs, bool)
+    keep[list(gauge)] = False
+    idx = np.nonzero(keep)[0]
+    r, A = prob.residual_jacobian(x)
+    lu = spla.splu(A[idx][:, idx].tocsc(), permc_spec="COLAMD")
+    del A
+    r0 = np.linalg.norm(r)
+    hist = [r0]
+    it = 0
+    while it < maxiter and hist[-1] > max(atol, rtol * r0):
+        x[idx] -= lu.solve(r[idx])
+        it += 1
+        r, _ = prob.residual_jacobian(x, want_jac=False)
+        hist.append(np.linalg.norm(r))
+        if verbose:
+            print(f"chord {it}: |r| = {hist[-1]:.3e}", flush=True)
+        if it > 3 and hist[-1] > 0.9 * hist[-2]:
             break
     return x, dict(nls_iters=it, residuals=hist)
 

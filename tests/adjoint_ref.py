@@ -23,6 +23,26 @@ def oracle_param_derivs(prob, x):
     return dR_dgamma, dR_dcw, fz
 
 
+def oracle_param_derivs_ab(prob, x):
+    """∂R/∂α and ∂R/∂β (global vectors) at x."""
+    L = O.lib()
+    nc = prob.cell_X.shape[0]
+    xc = np.ascontiguousarray(prob.cell_values(x))
+    da = np.zeros((nc, 129)); db = np.zeros((nc, 129))
+    sf, k1 = O._c_fluid(prob.fluid)
+    L.orc_param_derivs_ab(C.c_int64(nc), O._dp(prob.cell_X), O._dp(xc), C.byref(sf), O._dp(da), O._dp(db))
+    g = prob.gdofs
+    m = g >= 0
+    return (np.bincount(g[m], weights=da[m], minlength=prob.ndofs),
+            np.bincount(g[m], weights=db[m], minlength=prob.ndofs))
+
+
+def oracle_adjoint_ab(prob, lam, x):
+    """dJ/dα and dJ/dβ from the adjoint vector λ at x."""
+    dRa, dRb = oracle_param_derivs_ab(prob, x)
+    return -lam @ dRa, -lam @ dRb
+
+
 def oracle_adjoint(prob, dm, x, dJdx, gauge):
     """dJ/dγ, dJ/dcw, dJ/df_z(cell) at the solution x."""
     _, A = prob.residual_jacobian(x)

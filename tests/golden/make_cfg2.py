@@ -1,7 +1,10 @@
-"""Golden FP64 solution norms of the 32x32x3 stretched duct (Ha=100, Re=10, cw=0.1) from the
-CPU oracle's direct Newton (SuperLU), for the GPU parity test at that size.
+"""Golden FP64 solution of the 32x32x3 stretched duct (Ha=100, Re=10, cw=0.1) from the CPU
+oracle (FP64 assembly, one SuperLU factorization, chord iterations to the Newton root), for
+the GPU parity test at that size.
 
-    python tests/golden/make_cfg2.py      # writes tests/golden/cfg2_norms.json (minutes)
+    python tests/golden/make_cfg2.py
+writes tests/golden/cfg2_norms.json and tests/golden/cfg2_solution.npz (about half an hour
+on 8 cores: the SuperLU factorization of the 182,034-dof Jacobian dominates).
 """
 import json
 import os
@@ -25,7 +28,8 @@ def main():
     mesh, dm, params = hunt_case(**CFG2)
     prob = oracle_problem(mesh, dm, params)
     t = time.time()
-    x, info = O.newton_direct(prob, np.zeros(dm.ndofs), gauge=[dm.offsets["p"]], rtol=1e-13, maxiter=6)
+    x, info = O.newton_chord(prob, np.zeros(dm.ndofs), gauge=[dm.offsets["p"]], rtol=1e-14, maxiter=60,
+                             verbose=True)
     el = time.time() - t
     nrm = O.field_norms(mesh.cell_coords(), dm.cell_values(x))
     sp = dm.split(x)

@@ -77,3 +77,51 @@ def test_oracle_adjoint_pressure_drop_on_expansion():
     fm[c, 2] *= 1 - h
     fd = (g @ solve(dict(params, f_cell=fp))[1] - g @ solve(dict(params, f_cell=fm))[1]) / (2 * h * fz[c])
     assert abs(fd - dfz[c]) <= 1e-6 * abs(dfz).max(), (fd, dfz[c])
+
+
+def test_oracle_dJ_dHa_mhd_scaling():
+    """dJ/dHa of the expansion's pressure drop in the MHD scaling (α = Re/Ha², β = 1/Ha²,
+    γ = 1): the adjoint's dJ/dα and dJ/dβ through the chain rule of gbmhd.objectives against
+    central finite differences in Ha (step 1e-6 relative) with direct solves."""
+    from adjoint_ref import oracle_adjoint_ab
+    from gbmhd.objectives import ha_gradient, pressure_drop
+    from helpers import expansion_case
+    Ha, Re = 8.0, 4.0
+    mesh, dm, params = expansion_case(Ha=Ha, Re=Re)
+    gauge = [dm.offsets["phi"]]
+    g = pressure_drop(mesh, dm)
+
+    def solve(ha):
+        _, _, p = expansion_case(Ha=ha, Re=Re)
+        prob = oracle_problem(mesh, dm, p)
+        x, _ = O.newton_direct(prob, np.zeros(dm.ndofs), gauge=gauge, rtol=1e-14, maxiter=12)
+        return prob, x
+
+    prob, x = solve(Ha)
+    dgam, dcw, _, lam = oracle_adjoint(prob, dm, x, g, gauge)
+    dal, dbe = oracle_adjoint_ab(prob, lam, x)
+    dJ = np.array([dgam, dcw, dal, dbe])
+    ref = ha_gradient(dJ, Ha, Re, "mhd")
+    h = 1e-6
+    fd = (g @ solve(Ha * (1 + h))[1] - g @ solve(Ha * (1 - h))[1]) / (2 * h * Ha)
+    assert abs(fd - ref) <= 1e-6 * abs(ref), (fd, ref)
+    # each of dJ/dα and dJ/dβ on its own
+    for key, val in (("alpha", dal), ("beta", dbe)):
+        pp, pm = dict(params), dict(params)
+        pp[key] = params[key] * (1 + h)
+        pm[key] = params[key] * (1 - h)
+        Jp = g @ O.newton_direct(oracle_problem(mesh, dm, pp), np.zeros(dm.ndofs), gauge=gauge, rtol=1e-14,
+                                 maxiter=12)[0]
+        Jm = g @ O.newton_direct(oracle_problem(mesh, dm, pm), np.zeros(dm.ndofs), gauge=gauge, rtol=1e-14,
+                                 maxiter=12)[0]
+        fd = (Jp - Jm) / (2 * h * params[key])
+        assert abs(fd - val) <= 1e-6 * abs(val), (key, fd, val)
+
+
+def test_ha_gradient_chain_rule_cfd():
+    """CFD scaling: γ = Ha²/Re, so dJ/dHa = dJ/dγ · 2Ha/Re; unknown scalings are rejected."""
+    import pytest
+    from gbmhd.objectives import ha_gradient
+    assert ha_gradient(np.array([3.0, 0.0, 0.0, 0.0]), 50.0, 10.0, "cfd") == 3.0 * 2 * 50.0 / 10.0
+    with pytest.raises(ValueError):
+        ha_gradient(np.zeros(4), 1.0, 1.0, "other")

@@ -69,3 +69,44 @@ def test_badia2024_block_preconditioner_fp64(gpu_lib):
     for f in ("u", "j", "phi"):
         assert errs[f] <= 1e-7, (f, errs)
 
+
+
+def test_stagnation_safeguard_refactors_then_falls_back_to_fp64(gpu_lib, monkeypatch):
+    """The mixed-precision safeguard: the diagnostic stagnation test (GBMHD_STAG_ITERS=1,
+    GBMHD_STAG_REL=0) declares every FP32-preconditioned linear solve stagnated after one
+    iteration, so the first step refactors in FP32, stagnates again and moves to FP64 factors
+    for the rest of the solve.  Two refactorizations, and the solution still matches the
+    oracle's direct Newton."""
+    monkeypatch.setenv("GBMHD_STAG_ITERS", "1")
+    monkeypatch.setenv("GBMHD_STAG_REL", "0")
+    mesh, dm, params = hunt_case(**CASES["cfg1"])
+    prob = oracle_problem(mesh, dm, params)
+    xref, _ = O.newton_direct(prob, np.zeros(dm.ndofs), gauge=[dm.offsets["p"]], rtol=1e-13, maxiter=10)
+    ctx = gpu_context(mesh, dm, params)
+    x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), precision=1, max_newton=12, newton_rtol=1e-12,
+                                  newton_atol=0.0, restart=40, max_linear=400, linear_rtol=1e-4)
+    assert rc == 0 and rep["converged"], rep
+    assert rep["pc_refactorizations"] == 2, rep
+    for f, e in field_rel_errors(dm, x, xref).items():
+        assert e <= 1e-8, (f, e, rep)
+
+
+def test_sweep_wait_timeout_is_reported(gpu_lib, monkeypatch):
+    """A TMA sweep whose mbarrier wait gives up (here: a wait limit of zero spins, set through
+    the diagnostic GBMHD_SWEEP_WAIT_LIMIT before the factors are created) drains its copies in
+    flight, sets the device error flag, and the Newton step that used it fails with -3 and the
+    timeout message.  A new context (default limit) on the same device then solves normally."""
+    from gbmhd.lib import GbmhdError
+    mesh, dm, params = hunt_case(**CASES["cfg1"])
+    monkeypatch.setenv("GBMHD_SWEEP_WAIT_LIMIT", "0")
+    monkeypatch.setenv("GBMHD_STAG_ITERS", "100000")
+    ctx = gpu_context(mesh, dm, params)
+    with pytest.raises(GbmhdError, match="timed out"):
+        ctx.newton_solve(np.zeros(dm.ndofs), precision=1, max_newton=3, newton_rtol=1e-12, newton_atol=0.0,
+                         restart=20, max_linear=20, linear_rtol=1e-4)
+    monkeypatch.delenv("GBMHD_SWEEP_WAIT_LIMIT")
+    monkeypatch.delenv("GBMHD_STAG_ITERS")
+    ctx2 = gpu_context(mesh, dm, params)
+    x, rep, rc = ctx2.newton_solve(np.zeros(dm.ndofs), precision=1, max_newton=12, newton_rtol=1e-12,
+                                   newton_atol=0.0, restart=40, max_linear=400, linear_rtol=1e-4)
+    assert rc == 0 and rep["converged"], rep
