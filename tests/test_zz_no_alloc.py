@@ -72,7 +72,7 @@ def test_noalloc_without_thin_wall_facets(gpu_lib):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
-    mesh, dm, params = hunt_case(nc=(4, 4), nz=3, Ha=10.0, Re=10.0, cw=0.0, Lz=0.2)
+    mesh, dm, params = hunt_case(nc=(4, 4), nz=4, Ha=10.0, Re=10.0, cw=0.0, Lz=0.2)
     assert params["facets"] is None
     ctx = gpu_context(mesh, dm, params)
     x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), precision=0, max_newton=12, newton_rtol=1e-12,
