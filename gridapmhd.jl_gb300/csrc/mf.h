@@ -15,12 +15,16 @@
 // column-major matrices.
 //
 // Numeric phase (device): per level, fronts are gathered from the CSR values
-// (arrowheads), children's Schur complements are extend-added, and the
-// eliminated pivots are removed by blocked in-place Gauss-Jordan, whose rank-nb
-// updates are strided-batched GEMMs.  After it a front holds
-//   [ F11⁻¹        F11⁻¹F12        ]
-//   [ −F21F11⁻¹    F22 − F21F11⁻¹F12 ]
-// so both triangular sweeps of a solve are dense matrix-vector products.
+// (arrowheads), children's Schur complements are extend-added, and the eliminated
+// pivots are removed by a blocked right-looking LU whose diagonal NB-pivot blocks are
+// inverted with partial pivoting inside the block (panel and trailing updates are
+// strided-batched GEMMs).  After it a front holds
+//   [ D⁻¹ \ L11    U11 ]      D⁻¹: the inverses of the NB x NB diagonal blocks,
+//   [ L21          S   ]      L unit block-lower, U block-upper, S = F22 − L21 U12
+// (U12 is the upper-right block).  A solve is a forward substitution with L and a backward
+// one with U, per super-block of rows: a short chain of NB-block steps, then a dense GEMV.
+// Keeping the factors in LU form (rather than the explicit inverse of the eliminated block)
+// keeps FP32 rounding from being amplified by the conditioning of the whole block.
 #pragma once
 
 #include <cstdint>

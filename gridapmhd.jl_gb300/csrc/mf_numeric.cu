@@ -6,19 +6,17 @@
 #include <cstring>
 
 #include "mf.h"
+#include "tc_gemm.h"
 
 using namespace gbmhd;
 
 namespace {
 
-constexpr int NB = 64;   // Gauss-Jordan pivot block (inverted by one CTA)
+constexpr int NB = 64;   // diagonal pivot block (inverted by one CTA)
 constexpr long kSweepWaitDefault = 1L << 22;  // spin limit of the sweeps' mbarrier waits
-// panel: the trailing part of a front is updated once per PW pivots.  PW = 256 halves the
-// traffic again but multiplies the FP32 rounding of the panel's progressive inverse by the
-// conditioning of a 256-pivot block: at Ha = 500 (64x64x4) one solve in three then needed
-// 600+ FGMRES iterations instead of ~100.
+// panel: the trailing submatrix of a front takes one rank-PW update per PW pivots.
 constexpr int PW = 128;
-static_assert(PW % NB == 0 && PW <= 256 && (PW & (PW - 1)) == 0, "k_panel_rows maps one thread per panel row");
+static_assert(PW % NB == 0, "a panel holds whole pivot blocks");
 
 struct DevSym {
   int32_t* f_ne = nullptr;
@@ -48,25 +46,19 @@ struct MFNumeric {
   int precision = -1;          // precision of the stored factors
   void* F = nullptr;           // front storage (float or double)
   size_t F_bytes = 0;
-  void* Pbuf = nullptr;        // pivot inverses  [count][NB*NB]
-  void* Cbuf = nullptr;        // column blocks   [count][n*NB]
-  void* Tbuf = nullptr;        // row blocks      [count][NB*n]
-  void* T2buf = nullptr;
-  void* Rbuf = nullptr;        // panel rows before elimination   [count][PW*n]
-  void* Nbuf = nullptr;        // eliminated panel columns        [count][n*PW]
+  void* Pbuf = nullptr;        // diagonal-block inverses  [count][NB*NB]
+  void* Cbuf = nullptr;        // column block below a pivot block [count][n*NB]
   size_t work_bytes = 0;
-  double* tsave = nullptr;     // forward-sweep values of the eliminated dofs
-  double* ybuf = nullptr;      // backward-sweep accumulators (kept zero between solves)
+  double* tsave = nullptr;     // per front: E slots holding t, y and z of a solve
   int64_t* tsave_off = nullptr;  // per front
   int64_t tsave_len = 0;
   int32_t* d_err = nullptr;    // device-side status (singular pivot block)
-  int fp32_gemm_mode = 0;      // 0: BF16x9 emulated FP32, 1: plain FP32
   // TMA-staged sweeps (FP32 factors): one 3-D tensor map per level (rows x columns x fronts)
   std::vector<CUtensorMap> maps;
   std::vector<int> map_rows;      // row tile of each map
   std::vector<char> map_ok;
   const void* maps_base = nullptr;
-  float2* vpk = nullptr;            // packed vector segments of one level (transposed sweeps)
+  float2* vpk = nullptr;            // packed vector segments of one level (transposed GEMVs)
   bool scaled = false;              // factors are those of Dr A Dc (monolithic)
   double* d_dr = nullptr;           // [ndofs] row scales (powers of two)
   double* d_dc = nullptr;           // [ndofs] column scales
@@ -168,8 +160,7 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
       t += L.E;
     }
   M->tsave_len = t;
-  // forward reads rows E.. of the ne eliminated columns, backward rows 0..ne of the ne
-  // eliminated and nb boundary columns
+  // a solve reads L11 and L21 (forward), D⁻¹, U11 and U12 (backward): ne² + 2·ne·nb entries
   M->sweep_elems = 0;
   for (size_t f = 0; f < S.f_ne.size(); ++f) {
     const int64_t ne = S.f_ne[f], nb = S.f_nb[f];
@@ -188,22 +179,14 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
   MF_CUDA(cudaEventCreate(&M->ev1));
   if ((rc = upload(ctx, &M->tsave_off, toff))) return rc;
   MF_CUDA(cudaMalloc(&M->tsave, sizeof(double) * std::max<int64_t>(t, 1)));
-  MF_CUDA(cudaMalloc(&M->ybuf, sizeof(double) * std::max<int64_t>(t, 1)));
-  MF_CUDA(cudaMemset(M->ybuf, 0, sizeof(double) * std::max<int64_t>(t, 1)));
   MF_CUDA(cudaMalloc(&M->d_err, sizeof(int32_t)));
   if (cublasCreate(&M->blas) != CUBLAS_STATUS_SUCCESS) {
     ctx->err = "multifrontal: cublasCreate failed";
     return -2;
   }
   MF_BLAS(cublasSetStream(M->blas, ctx->stream));
-  // Front entries are finite (a singular pivot block raises the factorization error and a
-  // non-finite FGMRES residual ends the solve), so the BF16x9 emulation need not scan its
-  // operands for infinities and NaNs before every GEMM.
-  MF_BLAS(cublasSetEmulationSpecialValuesSupport(M->blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE));
   M->wait_limit = kSweepWaitDefault;
   if (const char* wl = std::getenv("GBMHD_SWEEP_WAIT_LIMIT")) M->wait_limit = std::max(0L, std::atol(wl));
-  const char* mode = std::getenv("GBMHD_FP32_GEMM");
-  M->fp32_gemm_mode = (mode && std::strcmp(mode, "fp32") == 0) ? 1 : 0;
   return 0;
 }
 
@@ -211,7 +194,7 @@ void mf_destroy(MFNumeric* M) {
   if (!M) return;
   void* ptrs[] = {M->d.f_ne, M->d.f_nb, M->d.f_off, M->d.elim_ptr, M->d.bnd_ptr, M->d.elim, M->d.bnd,
                   M->d.ah_src, M->d.ah_dst, M->d.child_list, M->d.ea_ptr, M->d.ea_pos, M->d.f_parent,
-                  M->d.f_level, M->d.reg_dst, M->d.reg_dof, M->F, M->Pbuf, M->Cbuf, M->Tbuf, M->T2buf, M->Rbuf, M->Nbuf, M->tsave, M->ybuf, M->tsave_off, M->d_err};
+                  M->d.f_level, M->d.reg_dst, M->d.reg_dof, M->F, M->Pbuf, M->Cbuf, M->tsave, M->tsave_off, M->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (M->blas) cublasDestroy(M->blas);
@@ -705,63 +688,29 @@ __global__ void __launch_bounds__(256) k_pivot_inverse_df_smem(const float* __re
     Pf[ti + j * NB] = (ti < kb && j < kb) ? __fadd_rn(Ah[ti + colsrc[j] * LD], Al[ti + colsrc[j] * LD]) : 0.0f;
 }
 
-// C = M[:, K] with the K rows zeroed (n x kb); Tb = M[K, c0 : c0+cw] (kb x cw).  Grid
-// (column groups, fronts).
+// ---- LU factorization helpers (the GEMMs of a panel step are strided-batched over the fronts)
+// dst[i + j·n] = M[r0 + i, c0 + j], i < nr, j < nc (per front; dst stride n·NB).
 template <typename T>
-__global__ void __launch_bounds__(256) k_gj_copy(const T* __restrict__ F, int64_t off, int n, int k, int kb, int c0,
-                                                 int cw, T* __restrict__ C, T* __restrict__ Tb) {
+__global__ void __launch_bounds__(256) k_copy_block(const T* __restrict__ F, int64_t off, int n, int r0, int nr,
+                                                    int c0, int nc, T* __restrict__ dst) {
   const int64_t f = blockIdx.y;
   const T* M = F + off + f * (int64_t)n * n;
-  T* Cf = C + f * (int64_t)n * NB;
-  T* Tf = Tb + f * (int64_t)NB * n;
-  for (int j = blockIdx.x; j < kb; j += gridDim.x)  // C: column k + j
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-      Cf[i + (int64_t)j * n] = (i >= k && i < k + kb) ? (T)0 : M[i + (int64_t)(k + j) * n];
-  const int r = threadIdx.x & (NB - 1);
-  for (int c = blockIdx.x * (256 / NB) + threadIdx.x / NB; c < cw; c += gridDim.x * (256 / NB))  // Tb: kb rows
-    if (r < kb) Tf[r + (int64_t)c * NB] = M[(k + r) + (int64_t)(c0 + c) * n];
+  T* D = dst + f * (int64_t)n * NB;
+  for (int j = blockIdx.x; j < nc; j += gridDim.x)
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) D[i + (int64_t)j * n] = M[(r0 + i) + (int64_t)(c0 + j) * n];
 }
 
-// M[K, c0 + c] = T2[:, c] for c < cw outside K; M[K, K] = P.
+// M[k + i, k + j] = P[i + j·NB], i, j < kb: the diagonal block's inverse goes into the front.
 template <typename T>
-__global__ void __launch_bounds__(256) k_gj_fix(T* __restrict__ F, int64_t off, int n, int k, int kb, int c0, int cw,
-                                                const T* __restrict__ T2, const T* __restrict__ P) {
-  const int64_t f = blockIdx.y;
+__global__ void __launch_bounds__(256) k_put_inverse(T* __restrict__ F, int64_t off, int n, int k, int kb,
+                                                     const T* __restrict__ P) {
+  const int64_t f = blockIdx.x;
   T* M = F + off + f * (int64_t)n * n;
-  const T* T2f = T2 + f * (int64_t)NB * n;
   const T* Pf = P + f * (int64_t)NB * NB;
-  const int r = threadIdx.x & (NB - 1);
-  for (int c = blockIdx.x * (256 / NB) + threadIdx.x / NB; c < cw; c += gridDim.x * (256 / NB))
-    if (r < kb) {
-      const int cc = c0 + c;
-      const bool inK = cc >= k && cc < k + kb;
-      M[(k + r) + (int64_t)cc * n] = inK ? Pf[r + (int64_t)(cc - k) * NB] : T2f[r + (int64_t)c * NB];
-    }
-}
-
-// Panel elimination helpers (panel = pivot columns [p, p + pw)):
-// R = M[p : p+pw, :] (pw x n, ld PW) before the panel is eliminated, and Nz = M[:, p : p+pw]
-// with the panel rows zeroed (n x pw, ld n) after it.
-template <typename T>
-__global__ void __launch_bounds__(256) k_panel_rows(const T* __restrict__ F, int64_t off, int n, int p, int pw,
-                                                    T* __restrict__ R) {
-  const int64_t f = blockIdx.y;
-  const T* M = F + off + f * (int64_t)n * n;
-  T* Rf = R + f * (int64_t)PW * n;
-  const int r = threadIdx.x & (PW - 1);
-  for (int c = blockIdx.x * (256 / PW) + threadIdx.x / PW; c < n; c += gridDim.x * (256 / PW))
-    if (r < pw) Rf[r + (int64_t)c * PW] = M[(p + r) + (int64_t)c * n];
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_panel_cols(const T* __restrict__ F, int64_t off, int n, int p, int pw,
-                                                    T* __restrict__ Nz) {
-  const int64_t f = blockIdx.y;
-  const T* M = F + off + f * (int64_t)n * n;
-  T* Nf = Nz + f * (int64_t)n * PW;
-  for (int j = blockIdx.x; j < pw; j += gridDim.x)
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-      Nf[i + (int64_t)j * n] = (i >= p && i < p + pw) ? (T)0 : M[i + (int64_t)(p + j) * n];
+  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+    const int i = e % kb, j = e / kb;
+    M[(k + i) + (int64_t)(k + j) * n] = Pf[i + j * NB];
+  }
 }
 
 // ------------------------------------------------------------------ solve kernels
@@ -913,195 +862,362 @@ __device__ __forceinline__ void warp_cols_dot(SweepAcc<float> (&acc)[NC], const 
   }
 }
 
-// Transposed sweeps (adjoint solves): a warp takes NC adjacent columns of a front and runs
-// down them together (each dot product is a contiguous column of the column-major front).
-// FP32 factors read the level's packed vector segments (vpk); FP64 factors stage theirs in
-// shared memory and use NC = 1.
-// forward, transposed: b[bnd_j] −= Σ_{i<ne} TR[i, j] t_i   (TR = rows 0..E of column E+j)
-template <typename T, int NC>
-__global__ void __launch_bounds__(256) k_fwd_gemv_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                    double* __restrict__ b, const double* __restrict__ tsave,
-                                                    const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
-                                                    const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_nb,
-                                                    const int32_t* __restrict__ f_ne, int64_t first, int n, int E,
-                                                    const float2* __restrict__ vpk) {
-  using V = typename SweepAcc<T>::V;
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  V* ts = reinterpret_cast<V*>(sm_raw);
-  const int64_t f = first + blockIdx.y;
-  const int nb = f_nb[f], ne = f_ne[f];
-  if constexpr (sizeof(T) != 4) {
-    const double* t = tsave + toff[f];
-    for (int i = threadIdx.x; i < ne; i += blockDim.x) ts[i] = SweepAcc<T>::pack(t[i]);
-    __syncthreads();
+// ---- LU-form sweeps
+// A front holds [D⁻¹\L11 , U11 ; L21 , S].  A solve runs over the eliminated block in
+// super-blocks of SB rows: a substitution chain over the NB-blocks inside a super-block
+// (k_tri_*), then a GEMV for the rows (forward) or the columns (backward) beyond it (k_rect*),
+// which for the last super-block is the coupling with the boundary.  Front index i < E
+// addresses the front's E slots of tsave (t, y and z of the sweeps) or x[elim[i]] (i < ne);
+// i ≥ E addresses b[bnd[i − E]] or x[bnd[i − E]] (i − E < nb).
+constexpr int SB = 512;
+static_assert(SB % NB == 0, "super-blocks hold whole NB-blocks");
+
+template <typename T>
+__device__ __forceinline__ double dsub(double a, const SweepAcc<T>& acc) { return a - acc.value(); }
+
+// acc += Σ_{u<cnt} m[u] v[u].  FP32 factors: the products with the vector's high and low
+// parts are summed with FP32 FMAs (at most 16 terms), then folded into the float-float
+// accumulator, as in the GEMV sweeps.
+template <typename T>
+__device__ __forceinline__ void acc_add_block(SweepAcc<T>& acc, const T* m, const typename SweepAcc<T>::V* v, int cnt);
+template <>
+__device__ __forceinline__ void acc_add_block<float>(SweepAcc<float>& acc, const float* m, const float2* v, int cnt) {
+  float h = 0.0f, l = 0.0f;
+  for (int u = 0; u < cnt; ++u) {
+    h = fmaf(m[u], v[u].x, h);
+    l = fmaf(m[u], v[u].y, l);
   }
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int j = (blockIdx.x * (blockDim.x / 32) + warp) * NC;
-  if (j >= nb) return;
-  const int ncols = min(NC, nb - j);
-  const T* colj = F + f_off[f] + (int64_t)(E + j) * n;
-  SweepAcc<T> acc[NC];
-  if constexpr (sizeof(T) == 4) {
-    warp_cols_dot<NC>(acc, colj, n, ncols, vpk + (int64_t)blockIdx.y * n, ne, lane);  // packed t of this front
-  } else {
-    static_assert(sizeof(T) == 4 || NC == 1, "FP64 transposed sweeps take one column per warp");
-    for (int i = lane; i < ne; i += 32) acc[0].add(colj[i], ts[i]);
-  }
-  const int32_t* bd = bnd + bnd_ptr[f];
-#pragma unroll
-  for (int c = 0; c < NC; ++c) {
-    acc[c].warp_reduce();
-    if (lane == 0 && c < ncols) atomicAdd(&b[bd[j + c]], -acc[c].value());
-  }
+  acc.merge(h, l);
+}
+template <>
+__device__ __forceinline__ void acc_add_block<double>(SweepAcc<double>& acc, const double* m, const double* v, int cnt) {
+  for (int u = 0; u < cnt; ++u) acc.a = fma(m[u], v[u], acc.a);
 }
 
-// backward, transposed: x[elim_i] = Σ_{c<ne} TL[c, i] t_c + Σ_{j<nb} BL[j, i] x_B[j]
-// (column i of the front: rows 0..E are TL, rows E.. are BL)
-template <typename T, int NC>
-__global__ void __launch_bounds__(256) k_bwd_gemv_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                    double* __restrict__ x, const double* __restrict__ tsave,
-                                                    const int64_t* __restrict__ toff, const int32_t* __restrict__ elim,
-                                                    const int64_t* __restrict__ elim_ptr, const int32_t* __restrict__ bnd,
-                                                    const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
-                                                    const int32_t* __restrict__ f_nb, int64_t first, int n, int E,
-                                                    const float2* __restrict__ vpk) {
+// Forward chain, unit lower: for the NB-blocks [k, k1) of [s0, s1) in order,
+//   t[k1:s1] −= M[k1:s1, k:k1] t[k:k1]      (t = the front's tsave slots, in place).
+// One CTA of SB threads per front; thread i keeps t[s0 + i] in FP64.
+template <typename T>
+__global__ void __launch_bounds__(SB) k_tri_fwd(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                int64_t first, int n, int s0, int s1) {
   using V = typename SweepAcc<T>::V;
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  V* vs = reinterpret_cast<V*>(sm_raw);  // [E] t, then [n-E] x_B
-  const int64_t f = first + blockIdx.y;
-  const int ne = f_ne[f], nb = f_nb[f];
-  if constexpr (sizeof(T) != 4) {
-    const double* t = tsave + toff[f];
-    const int32_t* bd = bnd + bnd_ptr[f];
-    for (int i = threadIdx.x; i < ne; i += blockDim.x) vs[i] = SweepAcc<T>::pack(t[i]);
-    for (int j = threadIdx.x; j < nb; j += blockDim.x) vs[E + j] = SweepAcc<T>::pack(x[bd[j]]);
-    __syncthreads();
-  }
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int i = (blockIdx.x * (blockDim.x / 32) + warp) * NC;
-  if (i >= ne) return;
-  const int ncols = min(NC, ne - i);
-  const T* coli = F + f_off[f] + (int64_t)i * n;
-  SweepAcc<T> acc[NC];
-  if constexpr (sizeof(T) == 4) {
-    const float2* v = vpk + (int64_t)blockIdx.y * n;  // packed [t ; x_B] of this front
-    warp_cols_dot<NC>(acc, coli, n, ncols, v, ne, lane);
-    warp_cols_dot<NC>(acc, coli + E, n, ncols, v + E, nb, lane);
-  } else {
-    static_assert(sizeof(T) == 4 || NC == 1, "FP64 transposed sweeps take one column per warp");
-    for (int c = lane; c < ne; c += 32) acc[0].add(coli[c], vs[c]);
-    for (int j = lane; j < nb; j += 32) acc[0].add(coli[E + j], vs[E + j]);
-  }
-  const int32_t* el = elim + elim_ptr[f];
-#pragma unroll
-  for (int c = 0; c < NC; ++c) {
-    acc[c].warp_reduce();
-    if (lane == 0 && c < ncols) x[el[i + c]] = acc[c].value();
-  }
-}
-
-// Packed (float-float) vector segments of a level's fronts for the transposed FP32 sweeps:
-// vpk[front][0, E) = t (zero beyond ne), and with x given, vpk[front][E, n) = x_B (zero
-// beyond nb).  One pass per level instead of every CTA staging its front's segment.
-__global__ void k_pack_vec(const double* __restrict__ tsave, const int64_t* __restrict__ toff,
-                           const double* __restrict__ x, const int32_t* __restrict__ bnd,
-                           const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
-                           const int32_t* __restrict__ f_nb, int64_t first, int n, int E, float2* __restrict__ vpk) {
+  __shared__ V vb[NB];
   const int64_t f = first + blockIdx.x;
-  const int ne = f_ne[f], nb = f_nb[f];
-  const double* t = tsave + toff[f];
-  float2* v = vpk + (int64_t)blockIdx.x * n;
-  for (int i = threadIdx.x; i < E; i += blockDim.x) v[i] = SweepAcc<float>::pack(i < ne ? t[i] : 0.0);
-  if (x) {
-    const int32_t* bd = bnd + bnd_ptr[f];
-    for (int j = threadIdx.x; j < n - E; j += blockDim.x) v[E + j] = SweepAcc<float>::pack(j < nb ? x[bd[j]] : 0.0);
+  const T* M = F + f_off[f];
+  double* t = tsave + toff[f];
+  const int r = s0 + (int)threadIdx.x;
+  double tr = r < s1 ? t[r] : 0.0;
+  for (int k = s0; k < s1; k += NB) {
+    const int k1 = min(k + NB, s1);
+    __syncthreads();  // the previous block's readers are done with vb
+    if (r >= k && r < k1) vb[r - k] = SweepAcc<T>::pack(tr);
+    __syncthreads();
+    if (r >= k1 && r < s1) {
+      SweepAcc<T> acc;
+      const T* row = M + r;
+      for (int c = k; c < k1; c += 16) {
+        const int cnt = min(16, k1 - c);
+        T m[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) m[u] = u < cnt ? __ldcs(row + (int64_t)(c + u) * n) : (T)0;
+        acc_add_block<T>(acc, m, vb + (c - k), cnt);
+      }
+      tr = dsub<T>(tr, acc);
+    }
+  }
+  if (r < s1) t[r] = tr;
+}
+
+// Backward chain, block upper with the stored block inverses: for the NB-blocks [k, k1) of
+// [s0, s1) in reverse,  x_k = D_k⁻¹ (z_k − M[k:k1, k1:s1] x[k1:s1]),  z = the tsave slots.
+// Writes x[elim[i]] for i < ne.  One CTA of NB × 8 threads per front: thread (i, g) sums the
+// columns ≡ g (mod 8) of row k + i; the eight partial sums meet in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(NB * 8) k_tri_bwd(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                    const double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                    double* __restrict__ x, const int32_t* __restrict__ elim,
+                                                    const int64_t* __restrict__ elim_ptr,
+                                                    const int32_t* __restrict__ f_ne, int64_t first, int n, int s0,
+                                                    int s1) {
+  using V = typename SweepAcc<T>::V;
+  __shared__ V xv[SB];              // the solved x of this super-block (packed)
+  __shared__ double part[8][NB];
+  __shared__ V rhs[NB];
+  const int64_t f = first + blockIdx.x;
+  const T* M = F + f_off[f];
+  const double* z = tsave + toff[f];
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int i = threadIdx.x % NB, g = threadIdx.x / NB;
+  const int nblk = (s1 - s0 + NB - 1) / NB;
+  for (int bk = nblk - 1; bk >= 0; --bk) {
+    const int k = s0 + bk * NB, k1 = min(k + NB, s1), kb = k1 - k;
+    // (1) r_i = z_i − Σ_{c ∈ [k1, s1)} M[k + i, c] x_c
+    SweepAcc<T> acc;
+    if (i < kb) {
+      const T* row = M + (k + i);
+      for (int cg = k1 + g; cg < s1; cg += 8 * 16) {
+        T m[16];
+        V v[16];
+        int cnt = 0;
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int c = cg + 8 * u;
+          if (c < s1) {
+            m[u] = __ldcs(row + (int64_t)c * n);
+            v[u] = xv[c - s0];
+            cnt = u + 1;
+          } else {
+            m[u] = (T)0;
+            v[u] = SweepAcc<T>::pack(0.0);
+          }
+        }
+        acc_add_block<T>(acc, m, v, cnt);
+      }
+    }
+    part[g][i] = acc.value();
+    __syncthreads();
+    if (g == 0 && i < kb) {
+      double s = 0.0;
+      for (int q = 0; q < 8; ++q) s += part[q][i];
+      rhs[i] = SweepAcc<T>::pack(z[k + i] - s);
+    }
+    __syncthreads();
+    // (2) x_{k+i} = Σ_c D⁻¹[i, c] r_c
+    SweepAcc<T> a2;
+    if (i < kb) {
+      const T* row = M + (k + i);
+      T m[8];
+      V v[8];
+      int cnt = 0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int c = g + 8 * u;
+        if (c < kb) {
+          m[u] = row[(int64_t)(k + c) * n];
+          v[u] = rhs[c];
+          cnt = u + 1;
+        } else {
+          m[u] = (T)0;
+          v[u] = SweepAcc<T>::pack(0.0);
+        }
+      }
+      acc_add_block<T>(a2, m, v, cnt);
+    }
+    part[g][i] = a2.value();
+    __syncthreads();
+    if (g == 0 && i < kb) {
+      double s = 0.0;
+      for (int q = 0; q < 8; ++q) s += part[q][i];
+      xv[k + i - s0] = SweepAcc<T>::pack(s);
+      if (k + i < ne) x[el[k + i]] = s;
+    }
+    __syncthreads();
   }
 }
 
-// Chunked sweeps: grid (row tiles, column chunks, fronts); each thread owns R consecutive
-// rows of its tile and reduces one chunk of `cols` columns, staged in shared memory; partial
-// sums are added atomically.  Row accesses are coalesced 16-byte vectors (column-major
-// fronts; E, B and n are multiples of 8, so every vector is aligned and rows up to the next
-// multiple of R stay inside the padded front).  The chunk width is chosen per level so that
-// levels with few fronts still fill the GPU.
-constexpr int SW_THREADS = 128;
-
-// forward: b[bnd_j] += Σ_{i<ne} M[E+j, i] t_i
+// Transposed forward chain (Uᵀ: block lower with D⁻ᵀ): for the NB-blocks [k, k1) of [s0, s1)
+// in order,  y_k = D_k⁻ᵀ t_k,  then t[k1:s1] −= M[k:k1, k1:s1]ᵀ y_k.  Column dot products, a
+// warp per column with the lanes down the (contiguous) column.  One CTA of 512 threads per
+// front.
 template <typename T>
-__global__ void __launch_bounds__(SW_THREADS) k_fwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                          double* __restrict__ b, const double* __restrict__ tsave,
-                                                          const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
-                                                          const int64_t* __restrict__ bnd_ptr,
-                                                          const int32_t* __restrict__ f_nb,
-                                                          const int32_t* __restrict__ f_ne, int64_t first, int n, int E,
-                                                          int cols) {
+__global__ void __launch_bounds__(512) k_tri_fwd_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                   double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                   int64_t first, int n, int s0, int s1) {
   using V = typename SweepAcc<T>::V;
-  constexpr int R = RowVec<T>::R;
-  extern __shared__ __align__(16) unsigned char sm_raw[];
-  V* ts = reinterpret_cast<V*>(sm_raw);
-  const int64_t f = first + blockIdx.z;
-  const int nb = f_nb[f];
-  const int j0 = (blockIdx.x * SW_THREADS + threadIdx.x) * R;
-  const int ne = f_ne[f];  // columns [ne, E) are padding
-  const int c0 = blockIdx.y * cols, c1 = min(ne, c0 + cols);
-  if (blockIdx.x * SW_THREADS * R >= nb || c0 >= ne) return;
-  const double* t = tsave + toff[f];
-  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) ts[c - c0] = SweepAcc<T>::pack(t[c]);
+  __shared__ double tt[SB];
+  __shared__ double yd[NB];
+  __shared__ V yb[NB];
+  const int64_t f = first + blockIdx.x;
+  const T* M = F + f_off[f];
+  double* t = tsave + toff[f];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
+  for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) tt[i] = t[s0 + i];
   __syncthreads();
-  if (j0 >= nb) return;
-  SweepAcc<T> acc[R];
-  strided_dot_rows<T>(acc, F + f_off[f] + E + j0 + (int64_t)c0 * n, n, ts, c1 - c0);
-  const int32_t* bd = bnd + bnd_ptr[f];
-#pragma unroll
-  for (int r = 0; r < R; ++r)
-    if (j0 + r < nb) atomicAdd(&b[bd[j0 + r]], acc[r].value());
+  for (int k = s0; k < s1; k += NB) {
+    const int k1 = min(k + NB, s1), kb = k1 - k;
+    for (int c = warp; c < kb; c += nw) {  // y_c = Σ_r D⁻¹[r, c] t_r
+      SweepAcc<T> acc;
+      const T* col = M + k + (int64_t)(k + c) * n;
+      for (int r = lane; r < kb; r += 32) acc.add(col[r], SweepAcc<T>::pack(tt[k - s0 + r]));
+      acc.warp_reduce();
+      if (lane == 0) yd[c] = acc.value();
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < kb) {
+      tt[k - s0 + threadIdx.x] = yd[threadIdx.x];
+      yb[threadIdx.x] = SweepAcc<T>::pack(yd[threadIdx.x]);
+    }
+    __syncthreads();
+    for (int c = k1 + warp; c < s1; c += nw) {  // t_c −= Σ_{r ∈ [k, k1)} M[r, c] y_r
+      SweepAcc<T> acc;
+      const T* col = M + k + (int64_t)c * n;
+      for (int r = lane; r < kb; r += 32) acc.add(col[r], yb[r]);
+      acc.warp_reduce();
+      if (lane == 0) tt[c - s0] = dsub<T>(tt[c - s0], acc);
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) t[s0 + i] = tt[i];
 }
 
-// backward: y_i = Σ_c M[i, c] v_c with v = [t ; −x_B], accumulated into ybuf (then scattered)
+// Transposed backward chain (Lᵀ: unit upper): for the NB-blocks [k, k1) of [s0, s1) in
+// reverse,  x_k = z_k − M[k1:s1, k:k1]ᵀ x[k1:s1];  writes x[elim[i]] for i < ne.
 template <typename T>
-__global__ void __launch_bounds__(SW_THREADS) k_bwd_chunk(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                          const double* __restrict__ x, const double* __restrict__ tsave,
-                                                          const int64_t* __restrict__ toff, const int32_t* __restrict__ bnd,
-                                                          const int64_t* __restrict__ bnd_ptr,
-                                                          const int32_t* __restrict__ f_ne,
-                                                          const int32_t* __restrict__ f_nb, double* __restrict__ ybuf,
-                                                          int64_t first, int n, int E, int cols) {
+__global__ void __launch_bounds__(512) k_tri_bwd_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                   const double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                   double* __restrict__ x, const int32_t* __restrict__ elim,
+                                                   const int64_t* __restrict__ elim_ptr,
+                                                   const int32_t* __restrict__ f_ne, int64_t first, int n, int s0,
+                                                   int s1) {
+  using V = typename SweepAcc<T>::V;
+  __shared__ V xv[SB];
+  const int64_t f = first + blockIdx.x;
+  const T* M = F + f_off[f];
+  const double* z = tsave + toff[f];
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
+  const int nblk = (s1 - s0 + NB - 1) / NB;
+  for (int bk = nblk - 1; bk >= 0; --bk) {
+    const int k = s0 + bk * NB, k1 = min(k + NB, s1), kb = k1 - k;
+    for (int c = warp; c < kb; c += nw) {
+      SweepAcc<T> acc;
+      const T* col = M + (int64_t)(k + c) * n;
+      for (int r = k1 + lane; r < s1; r += 32) acc.add(col[r], xv[r - s0]);
+      acc.warp_reduce();
+      if (lane == 0) {
+        const double v = dsub<T>(z[k + c], acc);
+        xv[k + c - s0] = SweepAcc<T>::pack(v);
+        if (k + c < ne) x[el[k + c]] = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Vector value at front index i: the E part from tsave (from_x = 0) or x[elim[i]] (from_x = 1,
+// zero for i ≥ ne); the boundary part from x[bnd[i − E]] (zero for i − E ≥ nb or x null).
+__device__ __forceinline__ double front_vec(int i, int E, int ne, int nb, const double* t, const double* x,
+                                            const int32_t* el, const int32_t* bd, int from_x) {
+  if (i < E) return from_x ? (i < ne ? x[el[i]] : 0.0) : t[i];
+  return (x && i - E < nb) ? x[bd[i - E]] : 0.0;
+}
+
+// out −= v at front index i: the E part into tsave, the boundary part into b[bnd[i − E]].
+__device__ __forceinline__ void front_sub(int i, int E, int nb, double* t, double* b, const int32_t* bd, double v) {
+  if (i < E) atomicAdd(&t[i], -v);
+  else if (i - E < nb) atomicAdd(&b[bd[i - E]], -v);
+}
+
+// Rectangular GEMV of the sweeps: out[r] −= Σ_{c ∈ [c0, c1)} M[r, c] v[c] for r ∈ [r0, r1).
+// Grid (row tiles, column chunks, fronts); a thread owns R consecutive rows (16-byte vector
+// loads of the column-major front; r0 a multiple of R) and reduces one chunk of `cols`
+// columns staged in shared memory; partial sums are added atomically.  The TMA-staged
+// version (k_rect_tma) takes the FP32 levels whose fronts are at least a box wide.
+constexpr int SW_THREADS = 128;
+template <typename T>
+__global__ void __launch_bounds__(SW_THREADS) k_rect(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                     double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                     const double* __restrict__ x, double* __restrict__ b,
+                                                     const int32_t* __restrict__ elim,
+                                                     const int64_t* __restrict__ elim_ptr,
+                                                     const int32_t* __restrict__ bnd, const int64_t* __restrict__ bnd_ptr,
+                                                     const int32_t* __restrict__ f_ne, const int32_t* __restrict__ f_nb,
+                                                     int64_t first, int n, int E, int r0, int r1, int c0, int c1,
+                                                     int cols, int from_x) {
   using V = typename SweepAcc<T>::V;
   constexpr int R = RowVec<T>::R;
   extern __shared__ __align__(16) unsigned char sm_raw[];
   V* vs = reinterpret_cast<V*>(sm_raw);
   const int64_t f = first + blockIdx.z;
   const int ne = f_ne[f], nb = f_nb[f];
-  const int i0 = (blockIdx.x * SW_THREADS + threadIdx.x) * R;
-  // virtual columns v in [0, ne + nb): v < ne -> column v, else column E + (v − ne)
-  const int c0 = blockIdx.y * cols, c1 = min(ne + nb, c0 + cols);
-  if (blockIdx.x * SW_THREADS * R >= ne || c0 >= ne + nb) return;
-  const double* t = tsave + toff[f];
+  const int j0 = r0 + (int)(blockIdx.x * SW_THREADS + threadIdx.x) * R;
+  const int ca = c0 + (int)blockIdx.y * cols, cb = min(c1, ca + cols);
+  if (r0 + (int)blockIdx.x * SW_THREADS * R >= r1 || ca >= cb) return;
+  double* t = tsave + toff[f];
+  const int32_t* el = elim + elim_ptr[f];
   const int32_t* bd = bnd + bnd_ptr[f];
-  for (int v = c0 + threadIdx.x; v < c1; v += blockDim.x)
-    vs[v - c0] = SweepAcc<T>::pack(v < ne ? t[v] : -x[bd[v - ne]]);
+  for (int c = ca + threadIdx.x; c < cb; c += blockDim.x)
+    vs[c - ca] = SweepAcc<T>::pack(front_vec(c, E, ne, nb, t, x, el, bd, from_x));
   __syncthreads();
-  if (i0 >= ne) return;
-  const T* M = F + f_off[f] + i0;
+  if (j0 >= r1) return;
   SweepAcc<T> acc[R];
-  const int va = min(c1, ne);
-  if (va > c0) strided_dot_rows<T>(acc, M + (int64_t)c0 * n, n, vs, va - c0);
-  const int vb = max(c0, ne);  // boundary columns: virtual v -> column E + (v − ne)
-  if (c1 > vb) strided_dot_rows<T>(acc, M + (int64_t)(E - ne + vb) * n, n, vs + (vb - c0), c1 - vb);
+  strided_dot_rows<T>(acc, F + f_off[f] + j0 + (int64_t)ca * n, n, vs, cb - ca);
 #pragma unroll
-  for (int r = 0; r < R; ++r)
-    if (i0 + r < ne) atomicAdd(&ybuf[toff[f] + i0 + r], acc[r].value());
+  for (int q = 0; q < R; ++q)
+    if (j0 + q < r1) front_sub(j0 + q, E, nb, t, b, bd, acc[q].value());
 }
 
-// ---- TMA-staged sweeps (FP32 factors)
+// Packed vector of front indices [r0, r1) for the transposed FP32 GEMVs: vpk[front][i − r0],
+// zero-padded to ld entries.
+__global__ void k_pack_front(const double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                             const double* __restrict__ x, const int32_t* __restrict__ elim,
+                             const int64_t* __restrict__ elim_ptr, const int32_t* __restrict__ bnd,
+                             const int64_t* __restrict__ bnd_ptr, const int32_t* __restrict__ f_ne,
+                             const int32_t* __restrict__ f_nb, int64_t first, int E, int r0, int r1, int ld,
+                             int from_x, float2* __restrict__ vpk) {
+  const int64_t f = first + blockIdx.x;
+  const int ne = f_ne[f], nb = f_nb[f];
+  const double* t = tsave + toff[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int32_t* bd = bnd + bnd_ptr[f];
+  float2* v = vpk + (int64_t)blockIdx.x * ld;
+  for (int i = r0 + threadIdx.x; i < r0 + ld; i += blockDim.x)
+    v[i - r0] = SweepAcc<float>::pack(i < r1 ? front_vec(i, E, ne, nb, t, x, el, bd, from_x) : 0.0);
+}
+
+// Transposed rectangular GEMV: out[c] −= Σ_{r ∈ [r0, r1)} M[r, c] v[r] for c ∈ [c0, c1).  A warp
+// takes NC adjacent columns and runs down them together (each a contiguous column segment);
+// FP32 factors read the packed vector (vpk, ld entries per front), FP64 factors gather theirs
+// into shared memory.
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) k_rect_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                const double* __restrict__ x, double* __restrict__ b,
+                                                const int32_t* __restrict__ elim, const int64_t* __restrict__ elim_ptr,
+                                                const int32_t* __restrict__ bnd, const int64_t* __restrict__ bnd_ptr,
+                                                const int32_t* __restrict__ f_ne, const int32_t* __restrict__ f_nb,
+                                                int64_t first, int n, int E, int r0, int r1, int c0, int c1, int ld,
+                                                int from_x, const float2* __restrict__ vpk) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  const int64_t f = first + blockIdx.y;
+  const int ne = f_ne[f], nb = f_nb[f];
+  double* t = tsave + toff[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int32_t* bd = bnd + bnd_ptr[f];
+  double* vd = reinterpret_cast<double*>(sm_raw);
+  if constexpr (sizeof(T) != 4) {
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) vd[i - r0] = front_vec(i, E, ne, nb, t, x, el, bd, from_x);
+    __syncthreads();
+  }
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int c = c0 + (int)(blockIdx.x * (blockDim.x / 32) + warp) * NC;
+  if (c >= c1) return;
+  const int ncols = min(NC, c1 - c);
+  const T* col = F + f_off[f] + r0 + (int64_t)c * n;
+  SweepAcc<T> acc[NC];
+  if constexpr (sizeof(T) == 4) {
+    warp_cols_dot<NC>(acc, col, n, ncols, vpk + (int64_t)blockIdx.y * ld, r1 - r0, lane);
+  } else {
+    static_assert(sizeof(T) == 4 || NC == 1, "FP64 transposed sweeps take one column per warp");
+    for (int r = lane; r < r1 - r0; r += 32) acc[0].add(col[r], vd[r]);
+  }
+#pragma unroll
+  for (int q = 0; q < NC; ++q) {
+    acc[q].warp_reduce();
+    if (lane == 0 && q < ncols) front_sub(c + q, E, nb, t, b, bd, acc[q].value());
+  }
+}
+
+// ---- TMA-staged GEMVs of the sweeps (FP32 factors)
 // A CTA owns a tile of `rows` rows (at most TS_ROWS, sized per level so that the tiles cover
-// the level's rows with little overhang) of one front and a chunk of its columns.  Thread 0
-// streams the chunk through shared memory in stages of TS_COLS columns with
-// cp.async.bulk.tensor (one 3-D tensor map per level: rows x columns x fronts), keeping
-// TS_STAGES stages in flight behind mbarriers; every thread reduces two rows of each staged
-// column in float-float arithmetic.  The forward sweep reads the boundary rows of the
-// eliminated columns, the backward sweep the eliminated rows of the eliminated columns
-// and of the boundary columns (two column segments, chunked separately).
+// the rows with little overhang) of one front and a chunk of its columns.  Thread 0 streams
+// the chunk through shared memory in stages of TS_COLS columns with cp.async.bulk.tensor (one
+// 3-D tensor map per level and direction: rows x columns x fronts), keeping TS_STAGES stages in
+// flight behind mbarriers; every thread reduces two rows of each staged column in float-float
+// arithmetic.
 constexpr int TS_ROWS = 256;
 constexpr int TS_COLS = 16;
 constexpr int TS_STAGES = 4;
@@ -1141,27 +1257,22 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// FWD: b[bnd_j] += Σ_{c<ne} M[E+j, c] t_c.   BWD: ybuf_i += Σ_v M[i, col(v)] w_v over v in this
-// CTA's chunk, w = [t ; −x_B], col(v) = v (v < ne) or E + (v − ne).
-//
-// The level's vector gather and scatter are folded in.  FWD reads t_c = b[elim_c] itself (the
-// level's eliminated dofs are not boundary dofs of any front of the level, so no CTA of the
-// launch writes them) and the CTAs of the first row tile save t for the backward sweep.  BWD
-// adds its partial sums straight into x[elim_i]; the solve zeroes x first.
-template <bool FWD>
-__global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant__ CUtensorMap map, int64_t first,
-                                                          int E, int rows, int cw, int chunks_a,
-                                                          double* __restrict__ b,
-                                                          double* __restrict__ x,
-                                                          double* __restrict__ tsave,
-                                                          const int64_t* __restrict__ toff,
-                                                          const int32_t* __restrict__ bnd,
-                                                          const int64_t* __restrict__ bnd_ptr,
-                                                          const int32_t* __restrict__ elim,
-                                                          const int64_t* __restrict__ elim_ptr,
-                                                          const int32_t* __restrict__ f_ne,
-                                                          const int32_t* __restrict__ f_nb, int32_t* err,
-                                                          long wait_limit) {
+// out[r] −= Σ_{c ∈ [c0, c1)} M[r, c] v[c] for r ∈ [r0, r1) (the semantics of k_rect) with the
+// front's columns streamed through shared memory by TMA.  CTA (row tile, column chunk,
+// front): thread 0 issues the stage copies; every wait is bounded (wait_limit spins), and a
+// wait that runs out makes the CTA wait (with the full limit) for its copies in flight, set
+// the error flag and return.
+__global__ void __launch_bounds__(TS_THREADS) k_rect_tma(const __grid_constant__ CUtensorMap map, int64_t first,
+                                                         int E, int r0, int r1, int c0, int c1, int rows, int cw,
+                                                         double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                         const double* __restrict__ x, double* __restrict__ b,
+                                                         const int32_t* __restrict__ elim,
+                                                         const int64_t* __restrict__ elim_ptr,
+                                                         const int32_t* __restrict__ bnd,
+                                                         const int64_t* __restrict__ bnd_ptr,
+                                                         const int32_t* __restrict__ f_ne,
+                                                         const int32_t* __restrict__ f_nb, int from_x, int32_t* err,
+                                                         long wait_limit) {
   extern __shared__ __align__(1024) unsigned char ts_raw[];
   float* tiles = reinterpret_cast<float*>(ts_raw);                  // [stage][column][row]
   float2* vs = reinterpret_cast<float2*>(ts_raw + (size_t)TS_STAGES * TS_COLS * rows * sizeof(float));  // [cw]
@@ -1170,21 +1281,10 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
   const int fl = blockIdx.z;
   const int64_t f = first + fl;
   const int ne = f_ne[f], nb = f_nb[f];
-  const int nrows = FWD ? nb : ne;
-  const int row0 = blockIdx.x * rows;
-  const bool seg_b = !FWD && (int)blockIdx.y >= chunks_a;
-  const int c0 = (seg_b ? (int)blockIdx.y - chunks_a : (int)blockIdx.y) * cw;
-  const int c1 = min(seg_b ? nb : ne, c0 + cw);
-  const int32_t* el = elim + elim_ptr[f];
-  if (FWD && blockIdx.x == 0) {  // save t for the backward sweep, also when the front has no rows here
-    double* ts = tsave + toff[f];
-    for (int c = c0 + (int)threadIdx.x; c < c1; c += blockDim.x) ts[c] = b[el[c]];
-  }
-  if (row0 >= nrows) return;
-  if (c0 >= c1) return;
-  const int ncol = c1 - c0;
-  const int pcol0 = seg_b ? E + c0 : c0;
-  const int prow0 = (FWD ? E : 0) + row0;
+  const int row0 = r0 + (int)blockIdx.x * rows;
+  const int ca = c0 + (int)blockIdx.y * cw, cb = min(c1, ca + cw);
+  if (row0 >= r1 || ca >= cb) return;
+  const int ncol = cb - ca;
   const int nst = (ncol + TS_COLS - 1) / TS_COLS;
   const uint32_t stage_bytes = TS_COLS * rows * sizeof(float);
   if (threadIdx.x == 0) {
@@ -1196,12 +1296,13 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
   if (threadIdx.x == 0)
     for (int s = 0; s < min(TS_STAGES, nst); ++s) {
       mbar_expect_tx(&full[s], stage_bytes);
-      tma_load_3d(tiles + (size_t)s * TS_COLS * rows, &map, prow0, pcol0 + s * TS_COLS, fl, &full[s]);
+      tma_load_3d(tiles + (size_t)s * TS_COLS * rows, &map, row0, ca + s * TS_COLS, fl, &full[s]);
     }
-  const double* t = tsave + toff[f];
+  double* t = tsave + toff[f];
+  const int32_t* el = elim + elim_ptr[f];
   const int32_t* bd = bnd + bnd_ptr[f];
   for (int c = threadIdx.x; c < ncol; c += blockDim.x)
-    vs[c] = SweepAcc<float>::pack(FWD ? b[el[c0 + c]] : seg_b ? -x[bd[c0 + c]] : t[c0 + c]);
+    vs[c] = SweepAcc<float>::pack(front_vec(ca + c, E, ne, nb, t, x, el, bd, from_x));
   __syncthreads();
   SweepAcc<float> a0, a1;
   const int r = 2 * threadIdx.x;
@@ -1213,8 +1314,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
       const int cn = min(TS_COLS, ncol - s * TS_COLS);
       // a stage's (at most 16) products are summed with FP32 FMAs, the high and low parts of
       // the vector separately, and the two short sums are folded into the float-float
-      // accumulators: ~3 instructions per factor entry instead of ~13 for float-float per
-      // product, with the rounding of 16-term FP32 sums only
+      // accumulators: ~3 instructions per factor entry
       float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f;
 #pragma unroll 4
       for (int c = 0; c < cn; ++c) {
@@ -1233,7 +1333,6 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
     __syncthreads();
     if (abort_flag) {
       if (threadIdx.x == 0) {  // let the copies in flight land before the CTA's shared memory is released
-        // (with the full limit, whatever limit the stage wait had)
         for (int s2 = s; s2 < min(nst, s + TS_STAGES); ++s2)
           mbar_wait_bounded(&full[s2 % TS_STAGES], (uint32_t)(s2 / TS_STAGES) & 1u, TS_WAIT_LIMIT);
         atomicExch(err, 1);
@@ -1242,36 +1341,12 @@ __global__ void __launch_bounds__(TS_THREADS) k_sweep_tma(const __grid_constant_
     }
     if (threadIdx.x == 0 && s + TS_STAGES < nst) {
       mbar_expect_tx(&full[buf], stage_bytes);
-      tma_load_3d(tiles + (size_t)buf * TS_COLS * rows, &map, prow0, pcol0 + (s + TS_STAGES) * TS_COLS, fl,
-                  &full[buf]);
+      tma_load_3d(tiles + (size_t)buf * TS_COLS * rows, &map, row0, ca + (s + TS_STAGES) * TS_COLS, fl, &full[buf]);
     }
   }
   const int i0 = row0 + r;
-  if (FWD) {
-    if (i0 < nb) atomicAdd(&b[bd[i0]], a0.value());
-    if (i0 + 1 < nb) atomicAdd(&b[bd[i0 + 1]], a1.value());
-  } else {
-    if (i0 < ne) atomicAdd(&x[el[i0]], a0.value());
-    if (i0 + 1 < ne) atomicAdd(&x[el[i0 + 1]], a1.value());
-  }
-}
-
-__global__ void k_zero_at(const int32_t* __restrict__ idx, int64_t cnt, double* __restrict__ x) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x)
-    x[idx[i]] = 0.0;
-}
-
-__global__ void k_bwd_scatter(double* __restrict__ x, double* __restrict__ ybuf, const int64_t* __restrict__ toff,
-                              const int32_t* __restrict__ elim, const int64_t* __restrict__ elim_ptr,
-                              const int32_t* __restrict__ f_ne, int64_t first) {
-  const int64_t f = first + blockIdx.x;
-  const int ne = f_ne[f];
-  const int32_t* el = elim + elim_ptr[f];
-  double* y = ybuf + toff[f];
-  for (int i = threadIdx.x; i < ne; i += blockDim.x) {
-    x[el[i]] = y[i];
-    y[i] = 0.0;  // ready for the next solve
-  }
+  if (i0 < r1) front_sub(i0, E, nb, t, b, bd, a0.value());
+  if (i0 + 1 < r1) front_sub(i0 + 1, E, nb, t, b, bd, a1.value());
 }
 
 // ------------------------------------------------------------------ host drivers
@@ -1302,9 +1377,9 @@ static int tma_rows(int nrows) {
   return std::min(TS_ROWS, std::max(32, (per + 31) / 32 * 32));
 }
 
-// Two maps per level over the FP32 fronts (forward: boundary rows, backward: eliminated
-// rows): dims (n rows, n columns, count fronts), box (rows, TS_COLS, 1).  A level whose
-// fronts are narrower than a box keeps the LDG sweeps.
+// Two maps per level over the FP32 fronts (forward and backward GEMVs of the sweeps): dims
+// (n rows, n columns, count fronts), box (rows, TS_COLS, 1).  A level whose fronts are
+// narrower than a box keeps the LDG GEMVs.
 static void build_sweep_maps(MFNumeric* M) {
   const MFSymbolic& S = M->S;
   const size_t nl = S.levels.size();
@@ -1320,7 +1395,9 @@ static void build_sweep_maps(MFNumeric* M) {
     if (L.n < TS_ROWS || L.count > (1 << 16)) continue;
     bool ok = true;
     for (int dir = 0; dir < 2; ++dir) {  // 0: forward (B rows), 1: backward (E rows)
-      const int rows = tma_rows(dir == 0 ? std::max(L.B, 1) : L.E);
+      // forward: the rows beyond a super-block (the boundary rows when E ≤ SB);
+      // backward: the rows of a super-block
+      const int rows = dir == 0 ? (L.E <= SB ? tma_rows(std::max(L.B, 1)) : TS_ROWS) : tma_rows(std::min(L.E, SB));
       const cuuint64_t dims[3] = {(cuuint64_t)L.n, (cuuint64_t)L.n, (cuuint64_t)L.count};
       const cuuint64_t strides[2] = {(cuuint64_t)L.n * sizeof(float), (cuuint64_t)L.n * L.n * sizeof(float)};
       const cuuint32_t box[3] = {(cuuint32_t)rows, TS_COLS, 1};
@@ -1345,24 +1422,25 @@ static int tma_cols(const gbmhd_ctx* ctx, int64_t rows, int tile_rows, int64_t n
   return (int)std::max<int64_t>(TS_COLS, std::min<int64_t>(cols, 1024));
 }
 
+// C = α·A·B + β·C for the fronts of a level (strided-batched, column-major).  FP32 factors use
+// the library's tensor-core GEMM (tc_gemm.cu); FP64 factors (the plain FP64 path) use cuBLAS
+// DGEMM.
 template <typename T>
-static cublasStatus_t gemm_sb(MFNumeric* M, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
-                              const T* alpha, const T* A, int lda, long long sA, const T* B, int ldb, long long sB,
-                              const T* beta, T* C, int ldc, long long sC, int batch) {
-  if constexpr (sizeof(T) == 8) {
-    return cublasGemmStridedBatchedEx(M->blas, ta, tb, m, n, k, alpha, A, CUDA_R_64F, lda, sA, B, CUDA_R_64F, ldb, sB,
-                                      beta, C, CUDA_R_64F, ldc, sC, batch, CUBLAS_COMPUTE_64F, CUBLAS_GEMM_DEFAULT);
+static int gemm(gbmhd_ctx* ctx, MFNumeric* M, int m, int n, int k, T alpha, const T* A, int lda, long long sA,
+                const T* B, int ldb, long long sB, T beta, T* C, int ldc, long long sC, int batch) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  if constexpr (sizeof(T) == 4) {
+    std::string msg;
+    const int rc = gbmhd::tc_gemm_f32(ctx->stream, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch,
+                                      M->d_err, &msg);
+    if (rc) ctx->err = "multifrontal: " + msg;
+    return rc;
   } else {
-    cublasComputeType_t ct = M->fp32_gemm_mode == 0 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9 : CUBLAS_COMPUTE_32F;
-    cublasStatus_t s = cublasGemmStridedBatchedEx(M->blas, ta, tb, m, n, k, alpha, A, CUDA_R_32F, lda, sA, B,
-                                                  CUDA_R_32F, ldb, sB, beta, C, CUDA_R_32F, ldc, sC, batch, ct,
-                                                  CUBLAS_GEMM_DEFAULT);
-    if (s != CUBLAS_STATUS_SUCCESS && M->fp32_gemm_mode == 0) {
-      M->fp32_gemm_mode = 1;  // emulation unavailable: plain FP32
-      s = cublasGemmStridedBatchedEx(M->blas, ta, tb, m, n, k, alpha, A, CUDA_R_32F, lda, sA, B, CUDA_R_32F, ldb, sB,
-                                     beta, C, CUDA_R_32F, ldc, sC, batch, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-    }
-    return s;
+    gbmhd::count_gemm();
+    MF_BLAS(cublasGemmStridedBatchedEx(M->blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &alpha, A, CUDA_R_64F, lda, sA,
+                                       B, CUDA_R_64F, ldb, sB, &beta, C, CUDA_R_64F, ldc, sC, batch,
+                                       CUBLAS_COMPUTE_64F, CUBLAS_GEMM_DEFAULT));
+    return 0;
   }
 }
 
@@ -1377,32 +1455,22 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
     MF_CUDA(cudaMalloc(&M->F, fbytes));
     M->F_bytes = fbytes;
   }
-  size_t wmax = 0, pmax = 0;
+  size_t wmax = 0, pbytes = 0;
   for (const MFLevel& L : S.levels) {
     wmax = std::max(wmax, (size_t)L.count * L.n * NB);
-    pmax = std::max(pmax, (size_t)L.count * L.n * PW);
+    pbytes = std::max(pbytes, (size_t)L.count * NB * NB);
   }
-  size_t pbytes = 0;
-  for (const MFLevel& L : S.levels) pbytes = std::max(pbytes, (size_t)L.count * NB * NB);
-  const size_t need = sizeof(T) * (3 * wmax + pbytes + 2 * pmax);
+  const size_t need = sizeof(T) * (wmax + pbytes);
   if (M->work_bytes < need) {
-    for (void* p : {M->Pbuf, M->Cbuf, M->Tbuf, M->T2buf, M->Rbuf, M->Nbuf})
+    for (void* p : {M->Pbuf, M->Cbuf})
       if (p) cudaFree(p);
     MF_CUDA(cudaMalloc(&M->Pbuf, sizeof(T) * std::max<size_t>(pbytes, 1)));
     MF_CUDA(cudaMalloc(&M->Cbuf, sizeof(T) * std::max<size_t>(wmax, 1)));
-    MF_CUDA(cudaMalloc(&M->Tbuf, sizeof(T) * std::max<size_t>(wmax, 1)));
-    MF_CUDA(cudaMalloc(&M->T2buf, sizeof(T) * std::max<size_t>(wmax, 1)));
-    MF_CUDA(cudaMalloc(&M->Rbuf, sizeof(T) * std::max<size_t>(pmax, 1)));
-    MF_CUDA(cudaMalloc(&M->Nbuf, sizeof(T) * std::max<size_t>(pmax, 1)));
     M->work_bytes = need;
   }
   T* F = reinterpret_cast<T*>(M->F);
   T* P = reinterpret_cast<T*>(M->Pbuf);
   T* C = reinterpret_cast<T*>(M->Cbuf);
-  T* Tb = reinterpret_cast<T*>(M->Tbuf);
-  T* T2 = reinterpret_cast<T*>(M->T2buf);
-  T* R = reinterpret_cast<T*>(M->Rbuf);
-  T* Nz = reinterpret_cast<T*>(M->Nbuf);
   MF_CUDA(cudaMemsetAsync(M->d_err, 0, sizeof(int32_t), ctx->stream));
   // level sizes on the device for the extend-add kernel
   std::vector<int> ln(S.levels.size()), le(S.levels.size());
@@ -1417,7 +1485,9 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
     const MFLevel& L = S.levels[l];
     const int n = L.n, E = L.E;
     const int cnt = (int)L.count;
-    MF_CUDA(cudaMemsetAsync(F + L.off, 0, sizeof(T) * (size_t)L.count * n * n, ctx->stream));
+    const long long sn = (long long)n * n;  // front stride
+    T* F0 = F + L.off;
+    MF_CUDA(cudaMemsetAsync(F0, 0, sizeof(T) * (size_t)L.count * n * n, ctx->stream));
     { k_pad_diag<T><<<cnt, 128, 0, ctx->stream>>>(F, L.off, L.count, n, E, M->d.f_ne, L.first); gbmhd::count_launch(); }
     const int64_t nah = L.ah_end - L.ah_begin;
     if (nah > 0) {
@@ -1439,20 +1509,13 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
                                                      M->d.f_parent, M->d.f_level, M->d.ea_ptr, M->d.ea_pos, d_ln, d_le); gbmhd::count_launch(); }
     }
     MF_CUDA(cudaGetLastError());
-    // Blocked in-place Gauss-Jordan over the eliminated pivots, by panels of PW pivots.
-    // Inside a panel, each 64-pivot block is eliminated from the panel's columns only (its
-    // inverse from k_pivot_inverse*, three small GEMMs); the rest of the front then takes the
-    // whole panel's elimination in one rank-PW update: M[:, rest] += Nz·R, M[P, rest] = N[P]·R
-    // (R = the panel rows before, N = the panel columns after).  Every pivot block still
-    // updates the whole front before the next panel, so F12, F21 and S come from the same
-    // progressive elimination as F11⁻¹.  (Forming them afterwards from the FP32 F11⁻¹ with
-    // three large GEMMs multiplies the inverse's rounding by κ(F11): at Ha = 500 that tripled
-    // the FGMRES iterations.)  One pass over a front per PW pivots instead of per 64 halves
-    // the HBM traffic of these memory-bound updates.
+    // Blocked right-looking LU of the eliminated block, by panels of PW pivots.  For each
+    // NB-pivot block K of the panel: D_K⁻¹ (k_pivot_inverse*, partial pivoting inside the
+    // block), L = M[below K, K]·D_K⁻¹, and the panel's later columns take L·M[K, ...].  The
+    // panel's later blocks then update their rows beyond the panel (U), and the trailing
+    // submatrix takes the whole panel in one rank-PW update.  D_K⁻¹ replaces M[K, K].
     for (int p = 0; p < E; p += PW) {
       const int pw = std::min(PW, E - p);
-      dim3 gr((unsigned)((n + 1) / 2), (unsigned)cnt);
-      { k_panel_rows<T><<<gr, 256, 0, ctx->stream>>>(F, L.off, n, p, pw, R); gbmhd::count_launch(); }
       for (int k = p; k < p + pw; k += NB) {
         const int kb = std::min(NB, p + pw - k);
         if constexpr (sizeof(T) == 4)
@@ -1464,36 +1527,45 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
           }
         else
           { k_pivot_inverse<T><<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
-        dim3 gc((unsigned)std::max(kb, (pw + 3) / 4), (unsigned)cnt);
-        { k_gj_copy<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, p, pw, C, Tb); gbmhd::count_launch(); }
-        MF_CUDA(cudaGetLastError());
-        // T2 = P · Tb  (kb x pw)
-        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, kb, pw, kb, &one, P, NB, (long long)NB * NB, Tb,
-                           NB, (long long)NB * n, &zero, T2, NB, (long long)NB * n, cnt));
-        // M[:, panel] -= C · T2   (n x pw)
-        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, pw, kb, &mone, C, n, (long long)n * NB, T2,
-                           NB, (long long)NB * n, &one, F + L.off + (int64_t)p * n, n, (long long)n * n, cnt));
-        // M[:, K] = −C · P  (n x kb)
-        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, kb, kb, &mone, C, n, (long long)n * NB, P,
-                           NB, (long long)NB * NB, &zero, F + L.off + (int64_t)k * n, n, (long long)n * n, cnt));
-        { k_gj_fix<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, p, pw, T2, P); gbmhd::count_launch(); }
+        const int rb = n - (k + kb);  // rows below the block (eliminated and boundary)
+        if (rb > 0) {
+          dim3 gc((unsigned)kb, (unsigned)cnt);
+          { k_copy_block<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, k + kb, rb, k, kb, C); gbmhd::count_launch(); }
+          MF_CUDA(cudaGetLastError());
+          T* Lk = F0 + (k + kb) + (int64_t)k * n;  // M[below, K]
+          const T* Dk = F0 + k + (int64_t)k * n;   // M[K, K], still the block itself
+          const long long sC = (long long)n * NB, sP = (long long)NB * NB;
+          int rc = 0;
+          // L = A·D⁻¹ with one refinement step for FP32 factors:  L₀ = A·D⁻¹,  R = A − L₀·D,
+          // L = L₀ + R·D⁻¹.  The FP32 inverse carries errors of κ(D)·2⁻²⁴; without the step they
+          // enter the Schur complements (FP32 emulation, 24x24x4 at Ha = 500: 15 → 5 FGMRES
+          // iterations to 1e-10 on the first Newton system).
+          if ((rc = gemm<T>(ctx, M, rb, kb, kb, one, C, n, sC, P, NB, sP, zero, Lk, n, sn, cnt))) return rc;
+          if constexpr (sizeof(T) == 4) {
+            if ((rc = gemm<T>(ctx, M, rb, kb, kb, mone, Lk, n, sn, Dk, n, sn, one, C, n, sC, cnt))) return rc;
+            if ((rc = gemm<T>(ctx, M, rb, kb, kb, one, C, n, sC, P, NB, sP, one, Lk, n, sn, cnt))) return rc;
+          }
+          const int cr = p + pw - (k + kb);  // the panel's later columns
+          if (cr > 0 && (rc = gemm<T>(ctx, M, rb, cr, kb, mone, Lk, n, sn, F0 + k + (int64_t)(k + kb) * n, n, sn,
+                                      one, F0 + (k + kb) + (int64_t)(k + kb) * n, n, sn, cnt)))
+            return rc;
+        }
+        { k_put_inverse<T><<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P); gbmhd::count_launch(); }
         MF_CUDA(cudaGetLastError());
       }
-      dim3 gn((unsigned)pw, (unsigned)cnt);
-      { k_panel_cols<T><<<gn, 256, 0, ctx->stream>>>(F, L.off, n, p, pw, Nz); gbmhd::count_launch(); }
-      MF_CUDA(cudaGetLastError());
-      // rest = columns [0, p) and [p + pw, n)
-      for (int side = 0; side < 2; ++side) {
-        const int c0 = side == 0 ? 0 : p + pw, cw = side == 0 ? p : n - (p + pw);
-        if (cw <= 0) continue;
-        // M[:, rest] += Nz · R[:, rest]   (n x cw, inner pw)
-        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, n, cw, pw, &one, Nz, n, (long long)n * PW,
-                           R + (int64_t)c0 * PW, PW, (long long)PW * n, &one, F + L.off + (int64_t)c0 * n, n,
-                           (long long)n * n, cnt));
-        // M[P, rest] = N[P, :] · R[:, rest]   (pw x cw; N[P, :] = the panel's pivot-block inverse)
-        gbmhd::count_gemm(); MF_BLAS(gemm_sb<T>(M, CUBLAS_OP_N, CUBLAS_OP_N, pw, cw, pw, &one,
-                           F + L.off + p + (int64_t)p * n, n, (long long)n * n, R + (int64_t)c0 * PW, PW,
-                           (long long)PW * n, &zero, F + L.off + p + (int64_t)c0 * n, n, (long long)n * n, cnt));
+      const int c0 = p + pw, rest = n - c0;
+      if (rest > 0) {
+        int rc = 0;
+        for (int k = p + NB; k < p + pw; k += NB) {  // U rows of the panel's later blocks
+          const int kb = std::min(NB, p + pw - k);
+          if ((rc = gemm<T>(ctx, M, kb, rest, k - p, mone, F0 + k + (int64_t)p * n, n, sn, F0 + p + (int64_t)c0 * n, n,
+                            sn, one, F0 + k + (int64_t)c0 * n, n, sn, cnt)))
+            return rc;
+        }
+        // trailing update: M[c0:, c0:] −= M[c0:, panel] · M[panel, c0:]
+        if ((rc = gemm<T>(ctx, M, rest, rest, pw, mone, F0 + c0 + (int64_t)p * n, n, sn, F0 + p + (int64_t)c0 * n, n,
+                          sn, one, F0 + c0 + (int64_t)c0 * n, n, sn, cnt)))
+          return rc;
       }
     }
   }
@@ -1503,7 +1575,8 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
   MF_CUDA(cudaMemcpyAsync(&herr, M->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
   MF_CUDA(cudaStreamSynchronize(ctx->stream));
   if (herr) {
-    ctx->err = "multifrontal: singular pivot block in the (u,j) factorization";
+    ctx->err = herr == 2 ? "multifrontal: a tensor-core GEMM wait timed out"
+                         : "multifrontal: singular pivot block in the factorization";
     return -3;
   }
   M->precision = sizeof(T) == 8 ? GBMHD_FP64 : GBMHD_MIXED;
@@ -1571,9 +1644,9 @@ int mf_factor(gbmhd_ctx* ctx, MFNumeric* M, int precision, int values, const dou
   return factor_scaled<double, double>(ctx, M, ctx->d_val64, d_reg);
 }
 
-// Column chunk of the chunked sweeps: wide enough that the partial-sum atomics stay a
-// small fraction of the factor reads, narrow enough that a level with few fronts still
-// launches about two waves of CTAs.
+// Column chunk of the LDG GEMVs: wide enough that the partial-sum atomics stay a small
+// fraction of the factor reads, narrow enough that a level with few fronts still launches
+// about two waves of CTAs.
 static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t fronts, int rows_per_cta) {
   const int64_t per_chunk = std::max<int64_t>(1, (rows + rows_per_cta - 1) / rows_per_cta) * std::max<int64_t>(1, fronts);
   const int64_t want = (int64_t)ctx->num_sms * 32;  // 2 waves of 16 resident 128-thread CTAs
@@ -1583,7 +1656,7 @@ static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t
   return (int)std::max<int64_t>(64, std::min<int64_t>(cols, 1024));
 }
 
-// Columns per warp of the transposed FP32 sweeps: 4 while a level still gives at least two
+// Columns per warp of the transposed FP32 GEMVs: 4 while a level still gives at least two
 // 256-thread CTAs per SM, else fewer (levels with few, large fronts).  FP64 factors: 1.
 #define GT_NC(k) (sizeof(T) == 4 ? (k) : 1)
 template <typename T>
@@ -1595,76 +1668,91 @@ static int gemv_t_cols(const gbmhd_ctx* ctx, int cols, int cnt) {
   return 1;
 }
 
+// One application of the factors: x = A⁻¹ b (or A⁻ᵀ b when tr) on the factorized dofs.  Per
+// level (forward bottom-up, backward top-down) and per super-block: the substitution chain
+// (k_tri_*), then the GEMV beyond the super-block (k_rect / k_rect_tma, or k_rect_t for the
+// transposed solve).  b is overwritten at the factorized dofs.
 template <typename T>
 static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool tr) {
   using V = typename SweepAcc<T>::V;
   const int rows_cta = SW_THREADS * RowVec<T>::R;
   const MFSymbolic& S = M->S;
   const T* F = reinterpret_cast<const T*>(M->F);
-  // the TMA backward sweeps add their partial sums into x directly: zero x at the dofs this
-  // factorization eliminates (the others, e.g. the p and φ blocks of the block-triangular
-  // preconditioner, hold the caller's values)
-  if (!tr && sizeof(T) == 4 && !S.elim.empty()) {
-    const int64_t ne_all = (int64_t)S.elim.size();
-    const unsigned gz = (unsigned)std::max<int64_t>(1, std::min<int64_t>((ne_all + 255) / 256, (int64_t)ctx->num_sms * 8));
-    { k_zero_at<<<gz, 256, 0, ctx->stream>>>(M->d.elim, ne_all, x); gbmhd::count_launch(); }
-  }
-  for (size_t l = 0; l < S.levels.size(); ++l) {
+  const DevSym& d = M->d;
+  // out[r] −= M[r0:r1, c0:c1] v   (dir: 0 forward map, 1 backward map)
+  auto rect = [&](size_t l, int dir, int r0, int r1, int c0, int c1, int from_x) -> int {
     const MFLevel& L = S.levels[l];
+    if (r1 <= r0 || c1 <= c0) return 0;
     const int cnt = (int)L.count;
-    const bool tma = !tr && sizeof(T) == 4 && M->map_ok[l];
-    if (!(tma && L.B > 0))  // the TMA forward sweep gathers t itself
-      { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first, L.E); gbmhd::count_launch(); }
-    if (L.B > 0) {
-      if (tma) {
-        const int rows = M->map_rows[2 * l];
-        const int cw = tma_cols(ctx, L.B, rows, L.E, cnt);
-        dim3 g((unsigned)((L.B + rows - 1) / rows), (unsigned)((L.E + cw - 1) / cw), (unsigned)cnt);
-        const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
-        MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-        { k_sweep_tma<true><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l], L.first, L.E, rows, cw, 0, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.elim, M->d.elim_ptr, M->d.f_ne, M->d.f_nb, M->d_sweep_err, M->wait_limit); gbmhd::count_launch(); }
-      } else if (!tr) {
-        const int cols = sweep_cols(ctx, L.B, L.E, cnt, rows_cta);
-        dim3 g((unsigned)((L.B + rows_cta - 1) / rows_cta), (unsigned)((L.E + cols - 1) / cols), (unsigned)cnt);
-        { k_fwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
+    if (sizeof(T) == 4 && M->map_ok[l]) {
+      const int rows = M->map_rows[2 * l + dir];
+      const int cw = tma_cols(ctx, r1 - r0, rows, c1 - c0, cnt);
+      dim3 g((unsigned)((r1 - r0 + rows - 1) / rows), (unsigned)((c1 - c0 + cw - 1) / cw), (unsigned)cnt);
+      const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
+      MF_CUDA(cudaFuncSetAttribute(k_rect_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      { k_rect_tma<<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l + dir], L.first, L.E, r0, r1, c0, c1, rows, cw,
+            M->tsave, M->tsave_off, x, b, d.elim, d.elim_ptr, d.bnd, d.bnd_ptr, d.f_ne, d.f_nb, from_x,
+            M->d_sweep_err, M->wait_limit); gbmhd::count_launch(); }
+    } else {
+      const int cols = sweep_cols(ctx, r1 - r0, c1 - c0, cnt, rows_cta);
+      dim3 g((unsigned)((r1 - r0 + rows_cta - 1) / rows_cta), (unsigned)((c1 - c0 + cols - 1) / cols), (unsigned)cnt);
+      { k_rect<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, b, d.elim,
+            d.elim_ptr, d.bnd, d.bnd_ptr, d.f_ne, d.f_nb, L.first, L.n, L.E, r0, r1, c0, c1, cols, from_x); gbmhd::count_launch(); }
+    }
+    MF_CUDA(cudaGetLastError());
+    return 0;
+  };
+  // out[c] −= M[r0:r1, c0:c1]ᵀ v
+  auto rect_t = [&](size_t l, int r0, int r1, int c0, int c1, int from_x) -> int {
+    const MFLevel& L = S.levels[l];
+    if (r1 <= r0 || c1 <= c0) return 0;
+    const int cnt = (int)L.count;
+    const int ld = (r1 - r0 + 3) / 4 * 4;
+    if (sizeof(T) == 4)
+      { k_pack_front<<<cnt, 256, 0, ctx->stream>>>(M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.bnd, d.bnd_ptr,
+            d.f_ne, d.f_nb, L.first, L.E, r0, r1, ld, from_x, M->vpk); gbmhd::count_launch(); }
+    const size_t sm = sizeof(T) == 4 ? 0 : sizeof(double) * (size_t)(r1 - r0);
+    const int nc = gemv_t_cols<T>(ctx, c1 - c0, cnt);
+    auto kf = nc == 4 ? k_rect_t<T, GT_NC(4)> : nc == 2 ? k_rect_t<T, GT_NC(2)> : k_rect_t<T, 1>;
+    MF_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
+    dim3 g((unsigned)((c1 - c0 + 8 * nc - 1) / (8 * nc)), (unsigned)cnt);
+    { kf<<<g, 256, sm, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, b, d.elim, d.elim_ptr, d.bnd, d.bnd_ptr,
+          d.f_ne, d.f_nb, L.first, L.n, L.E, r0, r1, c0, c1, ld, from_x, M->vpk); gbmhd::count_launch(); }
+    MF_CUDA(cudaGetLastError());
+    return 0;
+  };
+  int rc = 0;
+  for (size_t l = 0; l < S.levels.size(); ++l) {  // forward, bottom-up
+    const MFLevel& L = S.levels[l];
+    const int cnt = (int)L.count, n = L.n, E = L.E;
+    { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, d.elim, d.elim_ptr, d.f_ne, L.first, E); gbmhd::count_launch(); }
+    for (int s0 = 0; s0 < E; s0 += SB) {
+      const int s1 = std::min(E, s0 + SB);
+      if (!tr) {
+        { k_tri_fwd<T><<<cnt, SB, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, L.first, n, s0, s1); gbmhd::count_launch(); }
+        if ((rc = rect(l, 0, s1, n, s0, s1, 0))) return rc;
       } else {
-        const size_t sm = sizeof(T) == 4 ? 0 : sizeof(V) * L.E;
-        const int nc = gemv_t_cols<T>(ctx, L.B, cnt);
-        auto kf = nc == 4 ? k_fwd_gemv_t<T, GT_NC(4)> : nc == 2 ? k_fwd_gemv_t<T, GT_NC(2)> : k_fwd_gemv_t<T, 1>;
-        MF_CUDA(cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
-        if (sizeof(T) == 4)
-          { k_pack_vec<<<cnt, 256, 0, ctx->stream>>>(M->tsave, M->tsave_off, nullptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
-        dim3 g((unsigned)((L.B + 8 * nc - 1) / (8 * nc)), (unsigned)cnt);
-        { kf<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, b, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_nb, M->d.f_ne, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
+        { k_tri_fwd_t<T><<<cnt, 512, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, L.first, n, s0, s1); gbmhd::count_launch(); }
+        if ((rc = rect_t(l, s0, s1, s1, n, 0))) return rc;
       }
     }
     MF_CUDA(cudaGetLastError());
   }
-  for (int l = (int)S.levels.size() - 1; l >= 0; --l) {
+  for (int l = (int)S.levels.size() - 1; l >= 0; --l) {  // backward, top-down
     const MFLevel& L = S.levels[l];
-    const int cnt = (int)L.count;
-    if (!tr && sizeof(T) == 4 && M->map_ok[l]) {
-      const int rows = M->map_rows[2 * l + 1];
-      const int cw = tma_cols(ctx, L.E, rows, L.n, cnt);
-      const int ca = (L.E + cw - 1) / cw, cb = (L.B + cw - 1) / cw;
-      dim3 g((unsigned)((L.E + rows - 1) / rows), (unsigned)(ca + cb), (unsigned)cnt);
-      const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
-      MF_CUDA(cudaFuncSetAttribute(k_sweep_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      { k_sweep_tma<false><<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l + 1], L.first, L.E, rows, cw, ca, b, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.elim, M->d.elim_ptr, M->d.f_ne, M->d.f_nb, M->d_sweep_err, M->wait_limit); gbmhd::count_launch(); }
-    } else if (!tr) {
-      const int cols = sweep_cols(ctx, L.E, L.n, cnt, rows_cta);
-      dim3 g((unsigned)((L.E + rows_cta - 1) / rows_cta), (unsigned)((L.n + cols - 1) / cols), (unsigned)cnt);
-      { k_bwd_chunk<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, M->ybuf, L.first, L.n, L.E, cols); gbmhd::count_launch(); }
-      { k_bwd_scatter<<<cnt, 256, 0, ctx->stream>>>(x, M->ybuf, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.f_ne, L.first); gbmhd::count_launch(); }
-    } else {
-      const size_t sm = sizeof(T) == 4 ? 0 : sizeof(V) * L.n;
-      const int nc = gemv_t_cols<T>(ctx, L.E, cnt);
-      auto kb = nc == 4 ? k_bwd_gemv_t<T, GT_NC(4)> : nc == 2 ? k_bwd_gemv_t<T, GT_NC(2)> : k_bwd_gemv_t<T, 1>;
-      MF_CUDA(cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(sm, 1)));
-      if (sizeof(T) == 4)
-        { k_pack_vec<<<cnt, 256, 0, ctx->stream>>>(M->tsave, M->tsave_off, x, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
-      dim3 g((unsigned)((L.E + 8 * nc - 1) / (8 * nc)), (unsigned)cnt);
-      { kb<<<g, 256, sm, ctx->stream>>>(F, M->d.f_off, x, M->tsave, M->tsave_off, M->d.elim, M->d.elim_ptr, M->d.bnd, M->d.bnd_ptr, M->d.f_ne, M->d.f_nb, L.first, L.n, L.E, M->vpk); gbmhd::count_launch(); }
+    const int cnt = (int)L.count, n = L.n, E = L.E;
+    const int nsb = (E + SB - 1) / SB;
+    for (int sb = nsb - 1; sb >= 0; --sb) {
+      const int s0 = sb * SB, s1 = std::min(E, s0 + SB);
+      if (!tr) {
+        if ((rc = rect((size_t)l, 1, s0, s1, s1, n, 1))) return rc;
+        { k_tri_bwd<T><<<cnt, NB * 8, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr,
+              d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+      } else {
+        if ((rc = rect_t((size_t)l, s1, n, s0, s1, 1))) return rc;
+        { k_tri_bwd_t<T><<<cnt, 512, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr,
+              d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+      }
     }
     MF_CUDA(cudaGetLastError());
   }

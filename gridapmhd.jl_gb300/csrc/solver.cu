@@ -1036,3 +1036,45 @@ extern "C" int gbmhd_diag_uj_solve_error(gbmhd_ctx* ctx, const double* d_state, 
   return 0;
 }
 
+
+// Diagnostic: ‖y32 − y64‖/‖y64‖ for y = P⁻¹ b (or P⁻ᵀ b) with the monolithic preconditioner
+// factored in FP32 (from the FP32 Jacobian) and in FP64, for a seeded random b, the Jacobian
+// assembled at d_state.  Both factorizations are of the same regularised matrix, so the
+// difference measures the FP32 factors and sweeps in that direction.
+__global__ void k_rand_all(int64_t n, uint64_t seed, double* x) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(j + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    x[j] = (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+  }
+}
+
+extern "C" int gbmhd_diag_pc_compare(gbmhd_ctx* ctx, const double* d_state, int32_t transpose, double* err) {
+  if (!ctx || !d_state || !err) return -1;
+  if (!ctx->solver) ctx->solver = new Solver();
+  int rc = ensure_workspace(ctx, 4);
+  if (rc) return rc;
+  Solver* s = ctx->solver;
+  const int64_t n = ctx->ndofs;
+  if (!ctx->d_val32) S_CUDA(cudaMalloc(&ctx->d_val32, sizeof(float) * ctx->nnz));
+  if (!ctx->d_val64) S_CUDA(cudaMalloc(&ctx->d_val64, sizeof(double) * ctx->nnz));
+  double* b = s->V;
+  double* y32 = s->V + n;
+  double* y64 = s->V + 2 * n;
+  { k_rand_all<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 4242ull, b); gbmhd::count_launch(); }
+  if ((rc = gb_assemble_device(ctx, d_state, nullptr, 1, GBMHD_MIXED))) return rc;
+  if ((rc = setup_pc(ctx, GBMHD_MIXED, GBMHD_PC_MONOLITHIC, nullptr))) return rc;
+  if ((rc = apply_pc(ctx, GBMHD_MIXED, b, y32, transpose != 0))) return rc;
+  if ((rc = gb_assemble_device(ctx, d_state, nullptr, 1, GBMHD_FP64))) return rc;
+  if ((rc = setup_pc(ctx, GBMHD_FP64, GBMHD_PC_MONOLITHIC, nullptr))) return rc;
+  if ((rc = apply_pc(ctx, GBMHD_FP64, b, y64, transpose != 0))) return rc;
+  if ((rc = mf_check_sweeps(ctx, s->mf))) return rc;
+  double d2 = 0.0, r2 = 0.0;
+  { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, -1.0, y64, 1.0, y32); gbmhd::count_launch(); }
+  if ((rc = dot(ctx, s, y32, 1, y32, &d2))) return rc;
+  if ((rc = dot(ctx, s, y64, 1, y64, &r2))) return rc;
+  *err = std::sqrt(d2 / r2);
+  return 0;
+}

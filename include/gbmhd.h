@@ -247,6 +247,21 @@ int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double*
  *                                   that runs out drains its copies and makes the Newton step
  *                                   or the adjoint return -3 */
 
+/* Diagnostic: relative difference ‖y32 − y64‖/‖y64‖ of y = P⁻¹b (transpose = 0) or P⁻ᵀb
+ * (transpose = 1) for a seeded random b, with the monolithic preconditioner factored in FP32
+ * (from the FP32 Jacobian) and in FP64, both assembled at the device state d_state. */
+int gbmhd_diag_pc_compare(gbmhd_ctx* ctx, const double* d_state, int32_t transpose, double* err);
+
+/* Diagnostic: the FP32 strided-batched GEMM of the factorization's dense updates, on the
+ * tcgen05 tensor cores (three-way BF16 splits of each operand, six cross products, FP32
+ * accumulation in tensor memory): C = alpha·A·B + beta·C for `batch` column-major problems on
+ * device buffers (A m x k, B k x n, C m x n, strides sA, sB, sC between problems), 1 ≤ k ≤ 128.
+ * Synchronises the device; *status = 0, or 2 if a tensor-core wait timed out.  No counterpart
+ * in the reference (its dense kernels are UMFPACK's, src/main.jl:181-186). */
+int gbmhd_diag_tc_gemm(int32_t m, int32_t n, int32_t k, float alpha, const float* A, int32_t lda, int64_t sA,
+                       const float* B, int32_t ldb, int64_t sB, float beta, float* C, int32_t ldc, int64_t sC,
+                       int32_t batch, int32_t* status);
+
 /* Diagnostics: kernels launched by this library and cuBLAS GEMM calls it made
  * since it was loaded (all contexts together). */
 int gbmhd_counters(int64_t* kernel_launches, int64_t* gemm_calls);

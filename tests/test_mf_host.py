@@ -1,9 +1,8 @@
 """Host logic of the multifrontal factorization, checked on the CPU.
 
 The library's symbolic analysis (csrc/mf_symbolic.cpp, csrc/pattern.cpp) is compiled
-with g++ and run on small meshes; a numpy emulation of the numeric phase (front
-assembly, extend-add, Gauss-Jordan elimination, both sweeps) then has to solve the
-Jacobian assembled by the oracle."""
+with g++ and run on small meshes, and its structure is checked here; test_mf_lu_host.py
+emulates the numeric phase on it."""
 import ctypes as C
 import os
 import shutil
@@ -55,58 +54,6 @@ def symbolic(harness, mesh, dm, mono):
     return S
 
 
-def emulate(S, A, reg):
-    """Factor with the library's algorithm in FP64 and return the solve operator."""
-    lev, storage = S["levels"], int(S["sizes"][0])
-    F = np.zeros(storage)
-    n_of = lambda f: int(lev[S["f_level"][f]][2])
-    E_of = lambda f: int(lev[S["f_level"][f]][0])
-    for l in range(len(lev)):
-        E, B, n, first, count, off, ab, ae, cb, ce = (int(v) for v in lev[l])
-        for f in range(first, first + count):
-            for i in range(S["f_ne"][f], E):
-                F[S["f_off"][f] + i + i * n] = 1.0
-        F[S["ah_dst"][ab:ae]] = A.data[S["ah_src"][ab:ae]]
-        if l == len(lev) - 1:
-            F[S["reg_dst"]] += reg[S["reg_dof"]]
-        for c in S["child_list"][cb:ce]:
-            p, nc, Ec, nb = S["f_parent"][c], n_of(c), E_of(c), S["f_nb"][c]
-            Mc = F[S["f_off"][c]:S["f_off"][c] + nc * nc].reshape(nc, nc, order="F")
-            Mp = F[S["f_off"][p]:S["f_off"][p] + n_of(p) ** 2].reshape(n_of(p), n_of(p), order="F")
-            pos = S["ea_pos"][S["ea_ptr"][c]:S["ea_ptr"][c] + nb]
-            Mp[np.ix_(pos, pos)] += Mc[Ec:Ec + nb, Ec:Ec + nb]
-        for f in range(first, first + count):
-            M = F[S["f_off"][f]:S["f_off"][f] + n * n].reshape(n, n, order="F")
-            P = np.linalg.inv(M[:E, :E])
-            W = P @ M[:E, E:]
-            G = -M[E:, :E] @ P
-            Sc = M[E:, E:] - M[E:, :E] @ W
-            M[:E, :E], M[:E, E:], M[E:, :E], M[E:, E:] = P, W, G, Sc
-
-    def solve(b0):
-        b, x, ts = b0.copy(), np.zeros_like(b0), {}
-        for l in range(len(lev)):
-            E, B, n, first, count = (int(v) for v in lev[l][:5])
-            for f in range(first, first + count):
-                el = S["elim"][S["elim_ptr"][f]:S["elim_ptr"][f + 1]]
-                bd = S["bnd"][S["bnd_ptr"][f]:S["bnd_ptr"][f + 1]]
-                t = np.zeros(E)
-                t[:len(el)] = b[el]
-                ts[f] = t
-                M = F[S["f_off"][f]:S["f_off"][f] + n * n].reshape(n, n, order="F")
-                if len(bd):
-                    np.add.at(b, bd, M[E:E + len(bd), :E] @ t)
-        for l in range(len(lev) - 1, -1, -1):
-            E, B, n, first, count = (int(v) for v in lev[l][:5])
-            for f in range(first, first + count):
-                el = S["elim"][S["elim_ptr"][f]:S["elim_ptr"][f + 1]]
-                bd = S["bnd"][S["bnd_ptr"][f]:S["bnd_ptr"][f + 1]]
-                M = F[S["f_off"][f]:S["f_off"][f] + n * n].reshape(n, n, order="F")
-                x[el] = M[:len(el), :E] @ ts[f] - M[:len(el), E:E + len(bd)] @ x[bd]
-        return x
-    return solve
-
-
 @pytest.mark.parametrize("mono", [True, False])
 def test_symbolic_structure(harness, mono):
     mesh, dm, params = hunt_case(nc=(6, 5), nz=3, Ha=10.0, Re=10.0, cw=0.01, Lz=0.2)
@@ -150,26 +97,3 @@ def test_levels_keep_eliminated_and_boundary_dofs_apart(harness, mono, case):
         for f in range(first, first + count):
             b = S["bnd"][S["bnd_ptr"][f]:S["bnd_ptr"][f + 1]]
             assert len(np.unique(b)) == len(b)
-
-
-def test_emulated_factorization_solves_the_jacobian(harness):
-    from oracle import oracle as O  # noqa: F401
-    mesh, dm, params = hunt_case(nc=(6, 5), nz=3, Ha=10.0, Re=10.0, cw=0.01, Lz=0.2)
-    prob = oracle_problem(mesh, dm, params)
-    r, A = prob.residual_jacobian(np.zeros(dm.ndofs))
-    S = symbolic(harness, mesh, dm, True)
-    assert np.array_equal(S["rowptr"], A.indptr) and np.array_equal(S["col"], A.indices)
-    # root regularisation of the global constant modes, as the library does
-    X = mesh.cell_coords()
-    vol = np.abs(np.linalg.det(np.stack([X[:, 1] - X[:, 0], X[:, 2] - X[:, 0], X[:, 4] - X[:, 0]], 2)))
-    gd = dm.global_cell_dofs()
-    reg = np.zeros(dm.ndofs)
-    for k in range(4):
-        reg[gd[:, 81 + k]] = -vol / params["beta"] / 3
-    for k in range(8):
-        reg[gd[:, 121 + k]] = -vol / 27
-    solve = emulate(S, A, reg)
-    rng = np.random.default_rng(0)
-    x = rng.standard_normal(dm.ndofs)
-    K = A + sp.diags(np.where(np.isin(np.arange(dm.ndofs), S["reg_dof"]), reg, 0.0))
-    assert np.linalg.norm(solve(K @ x) - x) <= 1e-8 * np.linalg.norm(x)
