@@ -16,6 +16,7 @@ static std::atomic<int64_t> g_launches{0}, g_gemms{0};
 
 namespace gbmhd {
 void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 void count_gemm(int64_t n) { g_gemms.fetch_add(n, std::memory_order_relaxed); }
 }  // namespace gbmhd
 

@@ -91,6 +91,7 @@ bool touched(int a, int b);
 
 // Launch accounting (reported by gbmhd_counters).
 void count_launch(int64_t n = 1);
+int64_t launch_count();
 void count_gemm(int64_t n = 1);
 
 }  // namespace gbmhd

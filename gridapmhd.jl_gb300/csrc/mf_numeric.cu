@@ -67,6 +67,14 @@ struct MFNumeric {
   int32_t* d_sweep_err = nullptr;   // set by a sweep whose TMA wait timed out
   int32_t* h_sweep_err = nullptr;   // pinned copy, read at the next solve and by mf_check_sweeps
   long wait_limit = 0;              // spin limit of the sweeps' mbarrier waits
+  // one application of the monolithic factors as a CUDA graph per direction, on fixed buffers
+  double* gb = nullptr;             // [ndofs] right-hand side copy
+  double* gx = nullptr;             // [ndofs] solution
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  const void* g_factors[2] = {nullptr, nullptr};  // front storage the graph was captured on
+  int g_prec[2] = {-1, -1};
+  int64_t g_kernels[2] = {0, 0};    // kernels in each graph (launch accounting)
+  bool graphs_ok = true;            // capture failed once: launch directly
   // sweep timing: events around each solve, harvested when the next one starts
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool ev_pending = false;
@@ -204,6 +212,10 @@ void mf_destroy(MFNumeric* M) {
   if (M->d_sval) cudaFree(M->d_sval);
   if (M->d_sweep_err) cudaFree(M->d_sweep_err);
   if (M->h_sweep_err) cudaFreeHost(M->h_sweep_err);
+  for (int t = 0; t < 2; ++t)
+    if (M->gexec[t]) cudaGraphExecDestroy(M->gexec[t]);
+  if (M->gb) cudaFree(M->gb);
+  if (M->gx) cudaFree(M->gx);
   if (M->ev0) cudaEventDestroy(M->ev0);
   if (M->ev1) cudaEventDestroy(M->ev1);
   delete M;
@@ -714,16 +726,6 @@ __global__ void __launch_bounds__(256) k_put_inverse(T* __restrict__ F, int64_t 
 }
 
 // ------------------------------------------------------------------ solve kernels
-__global__ void k_fwd_gather(const double* __restrict__ b, double* __restrict__ tsave, const int64_t* __restrict__ toff,
-                             const int32_t* __restrict__ elim, const int64_t* __restrict__ elim_ptr,
-                             const int32_t* __restrict__ f_ne, int64_t first, int E) {
-  const int64_t f = first + blockIdx.x;
-  const int ne = f_ne[f];
-  const int32_t* el = elim + elim_ptr[f];
-  double* t = tsave + toff[f];
-  for (int i = threadIdx.x; i < E; i += blockDim.x) t[i] = i < ne ? b[el[i]] : 0.0;
-}
-
 // ---- accumulation of the sweeps
 // FP32 factors: the vector entries are split into two floats (hi + lo) and the products
 // are summed in float-float arithmetic (exact product error by FMA, Knuth's TwoSum for the
@@ -765,6 +767,12 @@ struct SweepAcc<float> {
       merge(oh, ol);
     }
   }
+  __device__ void warp_reduce8() {  // over aligned groups of 8 lanes
+    for (int o = 4; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, hi, o, 8), ol = __shfl_xor_sync(0xffffffffu, lo, o, 8);
+      merge(oh, ol);
+    }
+  }
   __device__ double value() const { return (double)hi + (double)lo; }
 };
 
@@ -777,6 +785,9 @@ struct SweepAcc<double> {
   __device__ void merge(const SweepAcc<double>& o) { a += o.a; }
   __device__ void warp_reduce() {
     for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  }
+  __device__ void warp_reduce8() {
+    for (int o = 4; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o, 8);
   }
   __device__ double value() const { return a; }
 };
@@ -894,168 +905,310 @@ __device__ __forceinline__ void acc_add_block<double>(SweepAcc<double>& acc, con
   for (int u = 0; u < cnt; ++u) acc.a = fma(m[u], v[u], acc.a);
 }
 
+template <typename VT>
+__device__ __forceinline__ VT vzero();
+template <>
+__device__ __forceinline__ float4 vzero<float4>() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+template <>
+__device__ __forceinline__ double2 vzero<double2>() { return make_double2(0.0, 0.0); }
+
+// acc[q] += Σ_u m[u][q] · vs[idx[u]] over the (at most 16) terms with ok[u].  FP32 factors: the
+// products with the vector's high and low parts are summed with FP32 FMAs and then folded into
+// the float-float accumulators (as in the GEMV sweeps); FP64 factors: FMAs.  vs is in shared
+// memory and read here, after the loads of m have been issued.
+template <typename T, int R, int N>
+__device__ __forceinline__ void fold_rows(SweepAcc<T> (&acc)[R], const typename RowVec<T>::type (&m)[N],
+                                          const typename SweepAcc<T>::V* vs, const int (&idx)[N],
+                                          const bool (&ok)[N]) {
+  static_assert(N <= 16, "at most 16 FP32 products per fold");
+  if constexpr (sizeof(T) == 4) {
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      float h = 0.0f, l = 0.0f;
+#pragma unroll
+      for (int u = 0; u < N; ++u)
+        if (ok[u]) {
+          const float mq = reinterpret_cast<const float*>(&m[u])[q];
+          const float2 v = vs[idx[u]];
+          h = fmaf(mq, v.x, h);
+          l = fmaf(mq, v.y, l);
+        }
+      acc[q].merge(h, l);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+#pragma unroll
+      for (int u = 0; u < N; ++u)
+        if (ok[u]) acc[q].a = fma(reinterpret_cast<const double*>(&m[u])[q], vs[idx[u]], acc[q].a);
+  }
+}
+
 // Forward chain, unit lower: for the NB-blocks [k, k1) of [s0, s1) in order,
 //   t[k1:s1] −= M[k1:s1, k:k1] t[k:k1]      (t = the front's tsave slots, in place).
-// One CTA of SB threads per front; thread i keeps t[s0 + i] in FP64.
-template <typename T>
-__global__ void __launch_bounds__(SB) k_tri_fwd(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                double* __restrict__ tsave, const int64_t* __restrict__ toff,
-                                                int64_t first, int n, int s0, int s1) {
+// A thread owns R consecutive rows (16-byte loads along the column-major front) and every
+// G-th column of a block, so that its loads of one step are issued together (one memory round
+// trip per step); with G > 1 the partial sums of a row meet in shared memory.  Levels with
+// many fronts use G = 1 (small CTAs, many per SM), levels with few fronts G = 4.  With gather
+// (the first super-block of a level) t is read from b[elim] for the whole front first.
+template <typename T, int G>
+__global__ void __launch_bounds__(SB / RowVec<T>::R * G, 512 / (SB / RowVec<T>::R * G)) k_tri_fwd(const T* __restrict__ F,
+                                                                  const int64_t* __restrict__ f_off,
+                                                                  double* __restrict__ tsave,
+                                                                  const int64_t* __restrict__ toff,
+                                                                  const double* __restrict__ b,
+                                                                  const int32_t* __restrict__ elim,
+                                                                  const int64_t* __restrict__ elim_ptr,
+                                                                  const int32_t* __restrict__ f_ne, int64_t first,
+                                                                  int n, int E, int s0, int s1, int gather) {
   using V = typename SweepAcc<T>::V;
+  using VT = typename RowVec<T>::type;
+  constexpr int R = RowVec<T>::R, RQ = SB / R, CPG = NB / G, CU = CPG < 16 ? CPG : 16;
   __shared__ V vb[NB];
+  __shared__ double part[G][SB];
   const int64_t f = first + blockIdx.x;
   const T* M = F + f_off[f];
   double* t = tsave + toff[f];
-  const int r = s0 + (int)threadIdx.x;
-  double tr = r < s1 ? t[r] : 0.0;
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int rq = threadIdx.x % RQ, g = threadIdx.x / RQ;
+  const int r0 = s0 + R * rq;
+  if (gather)
+    for (int i = threadIdx.x; i < E; i += blockDim.x)
+      if (i < s0 || i >= s1) t[i] = i < ne ? b[el[i]] : 0.0;
+  double tr[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int r = r0 + q;
+    tr[q] = (g == 0 && r < s1) ? (gather ? (r < ne ? b[el[r]] : 0.0) : t[r]) : 0.0;
+  }
   for (int k = s0; k < s1; k += NB) {
     const int k1 = min(k + NB, s1);
-    __syncthreads();  // the previous block's readers are done with vb
-    if (r >= k && r < k1) vb[r - k] = SweepAcc<T>::pack(tr);
-    __syncthreads();
-    if (r >= k1 && r < s1) {
-      SweepAcc<T> acc;
-      const T* row = M + r;
-      for (int c = k; c < k1; c += 16) {
-        const int cnt = min(16, k1 - c);
-        T m[16];
+    __syncthreads();  // the previous step's readers of vb and part are done
+    if (g == 0 && r0 >= k && r0 < k1)
 #pragma unroll
-        for (int u = 0; u < 16; ++u) m[u] = u < cnt ? __ldcs(row + (int64_t)(c + u) * n) : (T)0;
-        acc_add_block<T>(acc, m, vb + (c - k), cnt);
+      for (int q = 0; q < R; ++q) vb[r0 + q - k] = SweepAcc<T>::pack(tr[q]);
+    __syncthreads();
+    const bool active = r0 >= k1 && r0 < s1;  // k1 and s1 are multiples of R
+    SweepAcc<T> acc[R];
+    if (active)
+#pragma unroll 1
+      for (int u0 = 0; u0 < CPG; u0 += CU) {  // chunks of at most 16 vector loads per thread
+        VT m[CU];
+        int idx[CU];
+        bool ok[CU];
+#pragma unroll
+        for (int u = 0; u < CU; ++u) {
+          const int c = k + g + G * (u0 + u);
+          ok[u] = u0 + u < CPG && c < k1;
+          idx[u] = ok[u] ? c - k : 0;
+          m[u] = ok[u] ? __ldcs(reinterpret_cast<const VT*>(M + r0 + (int64_t)c * n)) : vzero<VT>();
+        }
+        fold_rows<T, R, CU>(acc, m, vb, idx, ok);
       }
-      tr = dsub<T>(tr, acc);
+    if constexpr (G > 1) {
+      if (active)
+#pragma unroll
+        for (int q = 0; q < R; ++q) part[g][r0 - s0 + q] = acc[q].value();
+      __syncthreads();
+      if (g == 0 && active)
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          double s = 0.0;
+#pragma unroll
+          for (int gg = 0; gg < G; ++gg) s += part[gg][r0 - s0 + q];
+          tr[q] -= s;
+        }
+    } else if (active) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) tr[q] -= acc[q].value();
     }
   }
-  if (r < s1) t[r] = tr;
+  if (g == 0)
+#pragma unroll
+    for (int q = 0; q < R; ++q)
+      if (r0 + q < s1) t[r0 + q] = tr[q];
 }
 
 // Backward chain, block upper with the stored block inverses: for the NB-blocks [k, k1) of
 // [s0, s1) in reverse,  x_k = D_k⁻¹ (z_k − M[k:k1, k1:s1] x[k1:s1]),  z = the tsave slots.
-// Writes x[elim[i]] for i < ne.  One CTA of NB × 8 threads per front: thread (i, g) sums the
-// columns ≡ g (mod 8) of row k + i; the eight partial sums meet in shared memory.
-template <typename T>
-__global__ void __launch_bounds__(NB * 8) k_tri_bwd(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                    const double* __restrict__ tsave, const int64_t* __restrict__ toff,
-                                                    double* __restrict__ x, const int32_t* __restrict__ elim,
-                                                    const int64_t* __restrict__ elim_ptr,
-                                                    const int32_t* __restrict__ f_ne, int64_t first, int n, int s0,
-                                                    int s1) {
+// Writes x[elim[i]] for i < ne.  A thread owns R consecutive rows of the block and every G-th
+// column; the U loads and the D⁻¹ loads of a step are issued together, and the G partial sums
+// of a row meet in shared memory.
+template <typename T, int G>
+__global__ void __launch_bounds__(NB / RowVec<T>::R * G, 512 / (NB / RowVec<T>::R * G)) k_tri_bwd(const T* __restrict__ F,
+                                                                  const int64_t* __restrict__ f_off,
+                                                                  const double* __restrict__ tsave,
+                                                                  const int64_t* __restrict__ toff,
+                                                                  double* __restrict__ x,
+                                                                  const int32_t* __restrict__ elim,
+                                                                  const int64_t* __restrict__ elim_ptr,
+                                                                  const int32_t* __restrict__ f_ne, int64_t first,
+                                                                  int n, int s0, int s1) {
   using V = typename SweepAcc<T>::V;
-  __shared__ V xv[SB];              // the solved x of this super-block (packed)
-  __shared__ double part[8][NB];
+  using VT = typename RowVec<T>::type;
+  constexpr int R = RowVec<T>::R, RQ = NB / R, CU = 16, CD = NB / G;
+  __shared__ V xv[SB];
+  __shared__ double part[G][NB];
   __shared__ V rhs[NB];
   const int64_t f = first + blockIdx.x;
   const T* M = F + f_off[f];
   const double* z = tsave + toff[f];
   const int ne = f_ne[f];
   const int32_t* el = elim + elim_ptr[f];
-  const int i = threadIdx.x % NB, g = threadIdx.x / NB;
+  const int rq = threadIdx.x % RQ, g = threadIdx.x / RQ;
+  const int i0 = R * rq;
   const int nblk = (s1 - s0 + NB - 1) / NB;
   for (int bk = nblk - 1; bk >= 0; --bk) {
     const int k = s0 + bk * NB, k1 = min(k + NB, s1), kb = k1 - k;
-    // (1) r_i = z_i − Σ_{c ∈ [k1, s1)} M[k + i, c] x_c
-    SweepAcc<T> acc;
-    if (i < kb) {
-      const T* row = M + (k + i);
-      for (int cg = k1 + g; cg < s1; cg += 8 * 16) {
-        T m[16];
-        V v[16];
-        int cnt = 0;
+    const bool live = i0 < kb;  // kb is a multiple of R
+    const T* rows = M + k + i0;
+    // D⁻¹ columns of this thread (independent of the chain: loaded with the first U chunk)
+    VT dm[CD];
+    int didx[CD];
+    bool dok[CD];
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int c = cg + 8 * u;
-          if (c < s1) {
-            m[u] = __ldcs(row + (int64_t)c * n);
-            v[u] = xv[c - s0];
-            cnt = u + 1;
-          } else {
-            m[u] = (T)0;
-            v[u] = SweepAcc<T>::pack(0.0);
-          }
-        }
-        acc_add_block<T>(acc, m, v, cnt);
-      }
+    for (int u = 0; u < CD; ++u) {
+      const int c = g + G * u;
+      dok[u] = live && c < kb;
+      didx[u] = dok[u] ? c : 0;
+      dm[u] = dok[u] ? *reinterpret_cast<const VT*>(rows + (int64_t)(k + c) * n) : vzero<VT>();
     }
-    part[g][i] = acc.value();
-    __syncthreads();
-    if (g == 0 && i < kb) {
-      double s = 0.0;
-      for (int q = 0; q < 8; ++q) s += part[q][i];
-      rhs[i] = SweepAcc<T>::pack(z[k + i] - s);
-    }
-    __syncthreads();
-    // (2) x_{k+i} = Σ_c D⁻¹[i, c] r_c
-    SweepAcc<T> a2;
-    if (i < kb) {
-      const T* row = M + (k + i);
-      T m[8];
-      V v[8];
-      int cnt = 0;
+    // (1) r = z_k − M[k:k1, k1:s1] x[k1:s1], by chunks of CU columns per thread
+    SweepAcc<T> acc[R];
+    if (live)
+#pragma unroll 1
+      for (int cb = k1 + g; cb < s1; cb += CU * G) {
+        VT m[CU];
+        int idx[CU];
+        bool ok[CU];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int c = g + 8 * u;
-        if (c < kb) {
-          m[u] = row[(int64_t)(k + c) * n];
-          v[u] = rhs[c];
-          cnt = u + 1;
-        } else {
-          m[u] = (T)0;
-          v[u] = SweepAcc<T>::pack(0.0);
+        for (int u = 0; u < CU; ++u) {
+          const int c = cb + G * u;
+          ok[u] = c < s1;
+          idx[u] = ok[u] ? c - s0 : 0;
+          m[u] = ok[u] ? __ldcs(reinterpret_cast<const VT*>(rows + (int64_t)c * n)) : vzero<VT>();
         }
+        fold_rows<T, R, CU>(acc, m, xv, idx, ok);
       }
-      acc_add_block<T>(a2, m, v, cnt);
-    }
-    part[g][i] = a2.value();
+    if (live)
+#pragma unroll
+      for (int q = 0; q < R; ++q) part[g][i0 + q] = acc[q].value();
     __syncthreads();
-    if (g == 0 && i < kb) {
-      double s = 0.0;
-      for (int q = 0; q < 8; ++q) s += part[q][i];
-      xv[k + i - s0] = SweepAcc<T>::pack(s);
-      if (k + i < ne) x[el[k + i]] = s;
+    if (g == 0 && live)
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        double s = 0.0;
+        for (int gg = 0; gg < G; ++gg) s += part[gg][i0 + q];
+        rhs[i0 + q] = SweepAcc<T>::pack(z[k + i0 + q] - s);
+      }
+    __syncthreads();
+    // (2) x_k = D⁻¹ r
+    SweepAcc<T> a2[R];
+    if (live) {
+      fold_rows<T, R, CD>(a2, dm, rhs, didx, dok);
+#pragma unroll
+      for (int q = 0; q < R; ++q) part[g][i0 + q] = a2[q].value();
     }
+    __syncthreads();
+    if (g == 0 && live)
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        double s = 0.0;
+        for (int gg = 0; gg < G; ++gg) s += part[gg][i0 + q];
+        xv[k + i0 + q - s0] = SweepAcc<T>::pack(s);
+        if (k + i0 + q < ne) x[el[k + i0 + q]] = s;
+      }
     __syncthreads();
   }
 }
 
 // Transposed forward chain (Uᵀ: block lower with D⁻ᵀ): for the NB-blocks [k, k1) of [s0, s1)
-// in order,  y_k = D_k⁻ᵀ t_k,  then t[k1:s1] −= M[k:k1, k1:s1]ᵀ y_k.  Column dot products, a
-// warp per column with the lanes down the (contiguous) column.  One CTA of 512 threads per
-// front.
+// in order,  y_k = D_k⁻ᵀ t_k,  then t[k1:s1] −= M[k:k1, k1:s1]ᵀ y_k.  Column dot products over
+// the block's NB rows: eight lanes per column (NB / 8 rows each, 16-byte loads), reduced with
+// shuffles; a CTA of 512 threads takes 64 columns per pass and issues the loads of all its
+// passes of a step together.  With gather, t is read from b[elim] for the whole front first.
+constexpr int TT_THREADS = 512;
 template <typename T>
-__global__ void __launch_bounds__(512) k_tri_fwd_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                   double* __restrict__ tsave, const int64_t* __restrict__ toff,
-                                                   int64_t first, int n, int s0, int s1) {
+__global__ void __launch_bounds__(TT_THREADS) k_tri_fwd_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                          double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                          const double* __restrict__ b,
+                                                          const int32_t* __restrict__ elim,
+                                                          const int64_t* __restrict__ elim_ptr,
+                                                          const int32_t* __restrict__ f_ne, int64_t first, int n,
+                                                          int E, int s0, int s1, int gather) {
   using V = typename SweepAcc<T>::V;
+  using VT = typename RowVec<T>::type;
+  constexpr int R = RowVec<T>::R, LV = NB / 8 / R;  // vector loads per lane and column
+  constexpr int NP = SB / (TT_THREADS / 8);          // passes of 64 columns over a super-block
   __shared__ double tt[SB];
-  __shared__ double yd[NB];
   __shared__ V yb[NB];
   const int64_t f = first + blockIdx.x;
   const T* M = F + f_off[f];
   double* t = tsave + toff[f];
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
-  for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) tt[i] = t[s0 + i];
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int j = threadIdx.x % 8, cs = threadIdx.x / 8;  // lane in the column, column slot
+  if (gather) {
+    for (int i = threadIdx.x; i < E; i += blockDim.x) {
+      const double v = i < ne ? b[el[i]] : 0.0;
+      if (i >= s0 && i < s1) tt[i - s0] = v;
+      else t[i] = v;
+    }
+  } else {
+    for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) tt[i] = t[s0 + i];
+  }
   __syncthreads();
   for (int k = s0; k < s1; k += NB) {
     const int k1 = min(k + NB, s1), kb = k1 - k;
-    for (int c = warp; c < kb; c += nw) {  // y_c = Σ_r D⁻¹[r, c] t_r
+    // (a) y_c = Σ_r D⁻¹[r, c] t_r, c = cs < kb
+    {
       SweepAcc<T> acc;
-      const T* col = M + k + (int64_t)(k + c) * n;
-      for (int r = lane; r < kb; r += 32) acc.add(col[r], SweepAcc<T>::pack(tt[k - s0 + r]));
-      acc.warp_reduce();
-      if (lane == 0) yd[c] = acc.value();
+      if (cs < kb) {
+        const T* col = M + k + (int64_t)(k + cs) * n;
+#pragma unroll
+        for (int u = 0; u < LV; ++u) {
+          const int r = R * (j + 8 * u);
+          if (r < kb) {
+            const VT m = *reinterpret_cast<const VT*>(col + r);
+#pragma unroll
+            for (int q = 0; q < R; ++q) acc.add(reinterpret_cast<const T*>(&m)[q], SweepAcc<T>::pack(tt[k - s0 + r + q]));
+          }
+        }
+      }
+      acc.warp_reduce8();
+      __syncthreads();  // every lane has read tt[k..k1)
+      if (j == 0 && cs < kb) {
+        const double y = acc.value();
+        tt[k - s0 + cs] = y;
+        yb[cs] = SweepAcc<T>::pack(y);
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    if ((int)threadIdx.x < kb) {
-      tt[k - s0 + threadIdx.x] = yd[threadIdx.x];
-      yb[threadIdx.x] = SweepAcc<T>::pack(yd[threadIdx.x]);
+    // (b) t_c −= Σ_{r ∈ [k, k1)} M[r, c] y_r, c ∈ [k1, s1): all passes' loads first
+    VT m[NP][LV];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const int c = k1 + cs + 64 * p;
+#pragma unroll
+      for (int u = 0; u < LV; ++u) {
+        const int r = R * (j + 8 * u);
+        m[p][u] = (c < s1 && r < kb) ? __ldcs(reinterpret_cast<const VT*>(M + k + r + (int64_t)c * n)) : vzero<VT>();
+      }
     }
-    __syncthreads();
-    for (int c = k1 + warp; c < s1; c += nw) {  // t_c −= Σ_{r ∈ [k, k1)} M[r, c] y_r
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const int c = k1 + cs + 64 * p;
       SweepAcc<T> acc;
-      const T* col = M + k + (int64_t)c * n;
-      for (int r = lane; r < kb; r += 32) acc.add(col[r], yb[r]);
-      acc.warp_reduce();
-      if (lane == 0) tt[c - s0] = dsub<T>(tt[c - s0], acc);
+#pragma unroll
+      for (int u = 0; u < LV; ++u) {
+        const int r = R * (j + 8 * u);
+        if (r < kb)
+#pragma unroll
+          for (int q = 0; q < R; ++q) acc.add(reinterpret_cast<const T*>(&m[p][u])[q], yb[r + q]);
+      }
+      acc.warp_reduce8();
+      if (j == 0 && c < s1) tt[c - s0] = dsub<T>(tt[c - s0], acc);
     }
     __syncthreads();
   }
@@ -1063,35 +1216,52 @@ __global__ void __launch_bounds__(512) k_tri_fwd_t(const T* __restrict__ F, cons
 }
 
 // Transposed backward chain (Lᵀ: unit upper): for the NB-blocks [k, k1) of [s0, s1) in
-// reverse,  x_k = z_k − M[k1:s1, k:k1]ᵀ x[k1:s1];  writes x[elim[i]] for i < ne.
+// reverse,  x_k = z_k − M[k1:s1, k:k1]ᵀ x[k1:s1];  writes x[elim[i]] for i < ne.  Eight lanes per
+// column, each taking every eighth 16-byte row group below the block; all loads of a step are
+// issued together.
 template <typename T>
-__global__ void __launch_bounds__(512) k_tri_bwd_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
-                                                   const double* __restrict__ tsave, const int64_t* __restrict__ toff,
-                                                   double* __restrict__ x, const int32_t* __restrict__ elim,
-                                                   const int64_t* __restrict__ elim_ptr,
-                                                   const int32_t* __restrict__ f_ne, int64_t first, int n, int s0,
-                                                   int s1) {
+__global__ void __launch_bounds__(TT_THREADS) k_tri_bwd_t(const T* __restrict__ F, const int64_t* __restrict__ f_off,
+                                                          const double* __restrict__ tsave,
+                                                          const int64_t* __restrict__ toff, double* __restrict__ x,
+                                                          const int32_t* __restrict__ elim,
+                                                          const int64_t* __restrict__ elim_ptr,
+                                                          const int32_t* __restrict__ f_ne, int64_t first, int n,
+                                                          int s0, int s1) {
   using V = typename SweepAcc<T>::V;
+  using VT = typename RowVec<T>::type;
+  constexpr int R = RowVec<T>::R, NL = (SB - NB) / (8 * R);  // row groups per lane, at most
   __shared__ V xv[SB];
   const int64_t f = first + blockIdx.x;
   const T* M = F + f_off[f];
   const double* z = tsave + toff[f];
   const int ne = f_ne[f];
   const int32_t* el = elim + elim_ptr[f];
-  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
+  const int j = threadIdx.x % 8, cs = threadIdx.x / 8;
   const int nblk = (s1 - s0 + NB - 1) / NB;
   for (int bk = nblk - 1; bk >= 0; --bk) {
     const int k = s0 + bk * NB, k1 = min(k + NB, s1), kb = k1 - k;
-    for (int c = warp; c < kb; c += nw) {
-      SweepAcc<T> acc;
-      const T* col = M + (int64_t)(k + c) * n;
-      for (int r = k1 + lane; r < s1; r += 32) acc.add(col[r], xv[r - s0]);
-      acc.warp_reduce();
-      if (lane == 0) {
-        const double v = dsub<T>(z[k + c], acc);
-        xv[k + c - s0] = SweepAcc<T>::pack(v);
-        if (k + c < ne) x[el[k + c]] = v;
+    SweepAcc<T> acc;
+    if (cs < kb) {
+      const T* col = M + (int64_t)(k + cs) * n;
+      VT m[NL];
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int r = k1 + R * (j + 8 * u);
+        m[u] = r < s1 ? __ldcs(reinterpret_cast<const VT*>(col + r)) : vzero<VT>();
       }
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int r = k1 + R * (j + 8 * u);
+        if (r < s1)
+#pragma unroll
+          for (int q = 0; q < R; ++q) acc.add(reinterpret_cast<const T*>(&m[u])[q], xv[r + q - s0]);
+      }
+    }
+    acc.warp_reduce8();
+    if (j == 0 && cs < kb) {
+      const double v = dsub<T>(z[k + cs], acc);
+      xv[k + cs - s0] = SweepAcc<T>::pack(v);
+      if (k + cs < ne) x[el[k + cs]] = v;
     }
     __syncthreads();
   }
@@ -1659,6 +1829,10 @@ static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t
 // Columns per warp of the transposed FP32 GEMVs: 4 while a level still gives at least two
 // 256-thread CTAs per SM, else fewer (levels with few, large fronts).  FP64 factors: 1.
 #define GT_NC(k) (sizeof(T) == 4 ? (k) : 1)
+// column groups of the chain kernels: FP64 factors (two rows per thread) use half as many,
+// so that a CTA keeps at most 512 threads
+#define TRI_G(k) (sizeof(T) == 4 ? (k) : 1)
+#define TRI_GB(k) (sizeof(T) == 4 ? (k) : (k) / 2)
 template <typename T>
 static int gemv_t_cols(const gbmhd_ctx* ctx, int cols, int cnt) {
   if (sizeof(T) != 4) return 1;
@@ -1725,14 +1899,19 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
   for (size_t l = 0; l < S.levels.size(); ++l) {  // forward, bottom-up
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count, n = L.n, E = L.E;
-    { k_fwd_gather<<<cnt, 256, 0, ctx->stream>>>(b, M->tsave, M->tsave_off, d.elim, d.elim_ptr, d.f_ne, L.first, E); gbmhd::count_launch(); }
+    const bool wide = cnt >= 2 * ctx->num_sms;  // many fronts: small CTAs, one wave
     for (int s0 = 0; s0 < E; s0 += SB) {
       const int s1 = std::min(E, s0 + SB);
+      const int gather = s0 == 0;  // the first chain reads t = b[elim] for the whole front
       if (!tr) {
-        { k_tri_fwd<T><<<cnt, SB, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, L.first, n, s0, s1); gbmhd::count_launch(); }
+        constexpr int R = RowVec<T>::R;
+        if (sizeof(T) == 8 || wide)
+          { k_tri_fwd<T, 1><<<cnt, SB / R, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
+        else
+          { k_tri_fwd<T, TRI_G(4)><<<cnt, SB / R * TRI_G(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
         if ((rc = rect(l, 0, s1, n, s0, s1, 0))) return rc;
       } else {
-        { k_tri_fwd_t<T><<<cnt, 512, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, L.first, n, s0, s1); gbmhd::count_launch(); }
+        { k_tri_fwd_t<T><<<cnt, TT_THREADS, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
         if ((rc = rect_t(l, s0, s1, s1, n, 0))) return rc;
       }
     }
@@ -1746,16 +1925,76 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       const int s0 = sb * SB, s1 = std::min(E, s0 + SB);
       if (!tr) {
         if ((rc = rect((size_t)l, 1, s0, s1, s1, n, 1))) return rc;
-        { k_tri_bwd<T><<<cnt, NB * 8, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr,
-              d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+        constexpr int RQ = NB / RowVec<T>::R;
+        if (cnt >= ctx->num_sms)
+          { k_tri_bwd<T, TRI_GB(8)><<<cnt, RQ * TRI_GB(8), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+        else
+          { k_tri_bwd<T, TRI_GB(32)><<<cnt, RQ * TRI_GB(32), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
       } else {
         if ((rc = rect_t((size_t)l, s1, n, s0, s1, 1))) return rc;
-        { k_tri_bwd_t<T><<<cnt, 512, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr,
+        { k_tri_bwd_t<T><<<cnt, TT_THREADS, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr,
               d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
       }
     }
     MF_CUDA(cudaGetLastError());
   }
+  return 0;
+}
+
+// The scaled solve: x = Dc (Dr A Dc)⁻¹ Dr b, or Dr (Dr A Dc)⁻ᵀ Dc b; b is overwritten.
+static int solve_scaled(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transpose) {
+  const int64_t nd = ctx->ndofs;
+  const unsigned gv = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nd + 255) / 256, (int64_t)ctx->num_sms * 8));
+  if (M->scaled) { k_scale_vec<<<gv, 256, 0, ctx->stream>>>(nd, transpose ? M->d_dc : M->d_dr, d_b); gbmhd::count_launch(); }
+  const int rc = M->precision == GBMHD_MIXED ? solve_impl<float>(ctx, M, d_b, d_x, transpose)
+                                             : solve_impl<double>(ctx, M, d_b, d_x, transpose);
+  if (rc) return rc;
+  if (M->scaled) { k_scale_vec<<<gv, 256, 0, ctx->stream>>>(nd, transpose ? M->d_dr : M->d_dc, d_x); gbmhd::count_launch(); }
+  return 0;
+}
+
+// Graph of one application on the fixed buffers gb → gx (monolithic factors: every dof of
+// x is written, so x's previous contents do not matter).  About 120 short kernels per
+// application at 64x64x4; replaying them as one graph removes the launch gaps between them.
+static int solve_graph(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool tr) {
+  const int64_t nd = ctx->ndofs;
+  const int t = tr ? 1 : 0;
+  if (!M->gb) {
+    MF_CUDA(cudaMalloc(&M->gb, sizeof(double) * std::max<int64_t>(nd, 1)));
+    MF_CUDA(cudaMalloc(&M->gx, sizeof(double) * std::max<int64_t>(nd, 1)));
+  }
+  MF_CUDA(cudaMemcpyAsync(M->gb, d_b, sizeof(double) * nd, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (!M->gexec[t] || M->g_factors[t] != M->F || M->g_prec[t] != M->precision) {
+    if (M->gexec[t]) cudaGraphExecDestroy(M->gexec[t]);
+    M->gexec[t] = nullptr;
+    const int64_t k0 = gbmhd::launch_count();
+    cudaGraph_t g = nullptr;
+    MF_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = solve_scaled(ctx, M, M->gb, M->gx, tr);
+    const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc || ec != cudaSuccess || !g) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      M->graphs_ok = false;  // launch directly from now on
+      if (rc) return rc;
+      return solve_scaled(ctx, M, d_b, d_x, tr);
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&M->gexec[t], g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      cudaGetLastError();
+      M->gexec[t] = nullptr;
+      M->graphs_ok = false;
+      return solve_scaled(ctx, M, d_b, d_x, tr);
+    }
+    M->g_kernels[t] = gbmhd::launch_count() - k0;
+    M->g_factors[t] = M->F;
+    M->g_prec[t] = M->precision;
+  } else {
+    gbmhd::count_launch(M->g_kernels[t]);
+  }
+  MF_CUDA(cudaGraphLaunch(M->gexec[t], ctx->stream));
+  MF_CUDA(cudaMemcpyAsync(d_x, M->gx, sizeof(double) * nd, cudaMemcpyDeviceToDevice, ctx->stream));
   return 0;
 }
 
@@ -1771,14 +2010,9 @@ int mf_solve(gbmhd_ctx* ctx, MFNumeric* M, double* d_b, double* d_x, bool transp
   harvest_sweep_time(M, false);
   const bool timed = !M->ev_pending && M->ev0 && M->ev1;
   if (timed) MF_CUDA(cudaEventRecord(M->ev0, ctx->stream));
-  const int64_t nd = ctx->ndofs;
-  const unsigned gv = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nd + 255) / 256, (int64_t)ctx->num_sms * 8));
-  // (Dr A Dc)⁻¹ = Dc⁻¹ A⁻¹ Dr⁻¹, so A⁻¹ b = Dc (Dr A Dc)⁻¹ Dr b and A⁻ᵀ b = Dr (Dr A Dc)⁻ᵀ Dc b
-  if (M->scaled) { k_scale_vec<<<gv, 256, 0, ctx->stream>>>(nd, transpose ? M->d_dc : M->d_dr, d_b); gbmhd::count_launch(); }
-  const int rc = M->precision == GBMHD_MIXED ? solve_impl<float>(ctx, M, d_b, d_x, transpose)
-                                             : solve_impl<double>(ctx, M, d_b, d_x, transpose);
+  const int rc = (M->S.monolithic && M->graphs_ok) ? solve_graph(ctx, M, d_b, d_x, transpose)
+                                                   : solve_scaled(ctx, M, d_b, d_x, transpose);
   if (rc) return rc;
-  if (M->scaled) { k_scale_vec<<<gv, 256, 0, ctx->stream>>>(nd, transpose ? M->d_dr : M->d_dc, d_x); gbmhd::count_launch(); }
   if (timed) {
     MF_CUDA(cudaEventRecord(M->ev1, ctx->stream));
     M->ev_pending = true;

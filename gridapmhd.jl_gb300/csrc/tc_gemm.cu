@@ -126,17 +126,19 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     const int gi = (isA ? i0 : j0) + row;
     const bool live = isA ? gi < m : gi < n;
     unsigned char* op = tc_smem + (isA ? 0 : 3 * PART_BYTES);
-    for (int kc = 0; kc < KH / 8; ++kc) {
-      float v[8];
+    // all KH loads of the row first (one memory round trip), then the splits
+    float v[KH];
+    const float* src = isA ? Ab + gi : Bb + (int64_t)gi * ldb;
+    const int64_t stride = isA ? lda : 1;
+    const int kn = live ? min(KH, k - kb0) : 0;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int kk = kb0 + kc * 8 + u;
-        v[u] = 0.0f;
-        if (live && kk < k) v[u] = isA ? Ab[gi + (int64_t)kk * lda] : Bb[kk + (int64_t)gi * ldb];
-      }
+    for (int u = 0; u < KH; ++u) v[u] = u < kn ? src[(int64_t)(kb0 + u) * stride] : 0.0f;
+#pragma unroll
+    for (int kc = 0; kc < KH / 8; ++kc) {
       // core matrix (row group row/8, K group kc): kc·(128·16) + (row/8)·128 + (row%8)·16
       const int off = kc * (TM * 16) + (row >> 3) * 128 + (row & 7) * 16;
-      split_store(v, op + off, op + PART_BYTES + off, op + 2 * PART_BYTES + off);
+      split_store(*reinterpret_cast<const float(*)[8]>(v + 8 * kc), op + off, op + PART_BYTES + off,
+                  op + 2 * PART_BYTES + off);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;");
