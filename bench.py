@@ -330,6 +330,80 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+# The sudden-expansion configuration: 3-D channel of rectangular section, inlet 1 (z) x 0.5 (y),
+# expanding 4x in y at x = 0, 2 upstream and 8 downstream; ~97k hexes graded toward the walls
+# and the step (more cells along the channel than across it: the factors of the 3-D separators
+# must fit in one GPU's memory); Ha = 1000, Re = 10, MHD scaling; parabolic inlet of mean 1 over
+# the outlet section; thin-wall law with cw = 0 (insulating) and τ = 100 on the walls; natural
+# outlet.  Objective: mean inlet pressure − mean outlet pressure.
+EXPANSION = dict(n_up=24, n_down=330, n_y_in=12, n_y_out=12, n_z=8, L_up=2.0, L_down=8.0, grading=4.0,
+                 Ha=1000.0, Re=10.0, thin_wall=(100.0, 0.0))
+
+
+def run_expansion(args):
+    """The expansion configuration end to end on the GPU: mixed-precision Newton solve, adjoint
+    gradient of the pressure drop w.r.t. (Ha, cw) and its check against central finite
+    differences of further Newton solves.  One JSON line; not part of the default bench."""
+    import torch
+    from gbmhd import _build, lib
+    from gbmhd.cases import expansion_case, gpu_context
+    from gbmhd.objectives import ha_gradient, pressure_drop
+    _build.build()
+    cfg = dict(EXPANSION)
+    if args.small:
+        cfg.update(n_up=6, n_down=40, n_y_in=6, n_y_out=6, n_z=6)
+    t0 = time.perf_counter()
+    mesh, dm, params = expansion_case(**cfg)
+    ctx = gpu_context(mesh, dm, params)
+    t_setup = time.perf_counter() - t0
+    g = pressure_drop(mesh, dm)
+    opts = dict(precision=lib.GBMHD_MIXED, max_newton=20, newton_rtol=1e-12, restart=100, max_linear=800,
+                linear_rtol=1e-3)
+    t = time.perf_counter()
+    x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), **opts)
+    t_newton = time.perf_counter() - t
+    sw_n, sw_s, sw_bytes = ctx.sweep_stats()
+    out = {"metric": "expansion: mixed Newton solve + pressure-drop adjoint (Ha, cw)", "impl": "ours",
+           "config": {"workload": f"sudden expansion {mesh.ncells} cells (nx {cfg['n_up']}+{cfg['n_down']}, "
+                                  f"ny {cfg['n_y_in']}+2x{cfg['n_y_out']}, nz {cfg['n_z']}), Ha=1000, Re=10, "
+                                  "MHD scaling, thin wall cw=0 tau=100", "ncells": mesh.ncells, "ndofs": dm.ndofs,
+                      "nnz": ctx.nnz},
+           "setup_host_s": t_setup, "newton_solve_s": t_newton, "newton_rc": int(rc), "report": rep,
+           "preconditioner": {"applications": sw_n, "ms_per_application": 1e3 * sw_s / sw_n if sw_n else None,
+                              "factor_gbytes_read_per_application": sw_bytes / 1e9}}
+    if rc != 0:
+        print(json.dumps(out))
+        return
+    Ha, Re = cfg["Ha"], cfg["Re"]
+    t = time.perf_counter()
+    dJ, lam, arep, arc = ctx.adjoint(x, g, with_cells=False, precision=lib.GBMHD_MIXED, restart=100, max_linear=800,
+                                     linear_rtol=1e-8)
+    t_adj = time.perf_counter() - t
+    dHa = ha_gradient(dJ, Ha, Re, "mhd")
+    out.update(adjoint_s=t_adj, adjoint_rc=int(arc), adjoint_linear_iters=arep["linear_iters"], J=float(g @ x),
+               dJ_dHa=dHa, dJ_dcw=float(dJ[1]), dJ_dalpha=float(dJ[2]), dJ_dbeta=float(dJ[3]))
+    # central finite differences (step 1e-6 relative in Ha, 1e-4 absolute in cw around 0)
+    def J_of(p):
+        ctx.set_params(p)
+        xs, r, c = ctx.newton_solve(x, **dict(opts, newton_rtol=0.0, newton_atol=0.0, max_newton=6,
+                                              linear_rtol=1e-10))
+        return float(g @ xs)
+    h = 1e-6
+    p0 = dict(params)
+    N = lambda ha: ha ** 2 / Re
+    pp = dict(p0, alpha=1.0 / N(Ha * (1 + h)), beta=1.0 / (Ha * (1 + h)) ** 2)
+    pm = dict(p0, alpha=1.0 / N(Ha * (1 - h)), beta=1.0 / (Ha * (1 - h)) ** 2)
+    fd_ha = (J_of(pp) - J_of(pm)) / (2 * h * Ha)
+    f = p0["facets"]
+    hc = 1e-4
+    fd_cw = (J_of(dict(p0, facets=dict(f, cw=f["cw"] + hc))) - J_of(dict(p0, facets=dict(f, cw=f["cw"] - hc)))) / (2 * hc)
+    ctx.set_params(p0)
+    out.update(fd_dJ_dHa=fd_ha, fd_dJ_dcw=fd_cw, rel_err_dHa=abs(fd_ha - dHa) / abs(dHa),
+               rel_err_dcw=abs(fd_cw - dJ[1]) / abs(dJ[1]) if dJ[1] != 0 else None,
+               gpu_mem_gb=torch.cuda.mem_get_info()[1] / 1e9 - torch.cuda.mem_get_info()[0] / 1e9)
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -340,7 +414,12 @@ def main():
     ap.add_argument("--small", action="store_true", help="32x32x3 duct (profiling captures)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the FP64-path and adjoint comparison")
+    ap.add_argument("--expansion", action="store_true",
+                    help="the sudden-expansion configuration (~97k cells, Ha=1000) instead of the duct bench")
     args = ap.parse_args()
+    if args.expansion:
+        run_expansion(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -194,6 +194,7 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
   }
   MF_BLAS(cublasSetStream(M->blas, ctx->stream));
   M->wait_limit = kSweepWaitDefault;
+  if (const char* gs = std::getenv("GBMHD_SWEEP_GRAPHS")) M->graphs_ok = std::atoi(gs) != 0;
   if (const char* wl = std::getenv("GBMHD_SWEEP_WAIT_LIMIT")) M->wait_limit = std::max(0L, std::atol(wl));
   return 0;
 }
@@ -944,34 +945,40 @@ __device__ __forceinline__ void fold_rows(SweepAcc<T> (&acc)[R], const typename 
   }
 }
 
+// float-float partial sums of a row, merged across the `width` lanes of an aligned group
+// (xor shuffles, FP32 arithmetic: GB300 issues FP64 at a small fraction of its FP32 rate)
+__device__ __forceinline__ void group_merge(SweepAcc<float>& a, int width) {
+  for (int o = width / 2; o > 0; o >>= 1) a.merge(__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o));
+}
+__device__ __forceinline__ void group_merge(SweepAcc<double>& a, int width) {
+  for (int o = width / 2; o > 0; o >>= 1) a.a += __shfl_xor_sync(0xffffffffu, a.a, o);
+}
+
 // Forward chain, unit lower: for the NB-blocks [k, k1) of [s0, s1) in order,
 //   t[k1:s1] −= M[k1:s1, k:k1] t[k:k1]      (t = the front's tsave slots, in place).
 // A thread owns R consecutive rows (16-byte loads along the column-major front) and every
 // G-th column of a block, so that its loads of one step are issued together (one memory round
-// trip per step); with G > 1 the partial sums of a row meet in shared memory.  Levels with
-// many fronts use G = 1 (small CTAs, many per SM), levels with few fronts G = 4.  With gather
-// (the first super-block of a level) t is read from b[elim] for the whole front first.
+// trip per step).  The G column groups of a row quad are adjacent lanes of one warp and merge
+// their float-float partial sums by shuffles.  Levels with many fronts use G = 1 (small CTAs,
+// many per SM), levels with few fronts G = 4.  With gather (the first super-block of a level)
+// t is read from b[elim] for the whole front first.
 template <typename T, int G>
-__global__ void __launch_bounds__(SB / RowVec<T>::R * G, 512 / (SB / RowVec<T>::R * G)) k_tri_fwd(const T* __restrict__ F,
-                                                                  const int64_t* __restrict__ f_off,
-                                                                  double* __restrict__ tsave,
-                                                                  const int64_t* __restrict__ toff,
-                                                                  const double* __restrict__ b,
-                                                                  const int32_t* __restrict__ elim,
-                                                                  const int64_t* __restrict__ elim_ptr,
-                                                                  const int32_t* __restrict__ f_ne, int64_t first,
-                                                                  int n, int E, int s0, int s1, int gather) {
+__global__ void __launch_bounds__(SB / RowVec<T>::R * G, 512 / (SB / RowVec<T>::R * G)) k_tri_fwd(
+    const T* __restrict__ F, const int64_t* __restrict__ f_off, double* __restrict__ tsave,
+    const int64_t* __restrict__ toff, const double* __restrict__ b, const int32_t* __restrict__ elim,
+    const int64_t* __restrict__ elim_ptr, const int32_t* __restrict__ f_ne, int64_t first, int n, int E, int s0,
+    int s1, int gather) {
   using V = typename SweepAcc<T>::V;
   using VT = typename RowVec<T>::type;
-  constexpr int R = RowVec<T>::R, RQ = SB / R, CPG = NB / G, CU = CPG < 16 ? CPG : 16;
+  constexpr int R = RowVec<T>::R, CPG = NB / G, CU = CPG < 16 ? CPG : 16;
+  static_assert(32 % G == 0, "the column groups of a row quad share a warp");
   __shared__ V vb[NB];
-  __shared__ double part[G][SB];
   const int64_t f = first + blockIdx.x;
   const T* M = F + f_off[f];
   double* t = tsave + toff[f];
   const int ne = f_ne[f];
   const int32_t* el = elim + elim_ptr[f];
-  const int rq = threadIdx.x % RQ, g = threadIdx.x / RQ;
+  const int g = threadIdx.x % G, rq = threadIdx.x / G;  // column group (adjacent lanes), row quad
   const int r0 = s0 + R * rq;
   if (gather)
     for (int i = threadIdx.x; i < E; i += blockDim.x)
@@ -980,11 +987,11 @@ __global__ void __launch_bounds__(SB / RowVec<T>::R * G, 512 / (SB / RowVec<T>::
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     const int r = r0 + q;
-    tr[q] = (g == 0 && r < s1) ? (gather ? (r < ne ? b[el[r]] : 0.0) : t[r]) : 0.0;
+    tr[q] = r < s1 ? (gather ? (r < ne ? b[el[r]] : 0.0) : t[r]) : 0.0;
   }
   for (int k = s0; k < s1; k += NB) {
     const int k1 = min(k + NB, s1);
-    __syncthreads();  // the previous step's readers of vb and part are done
+    __syncthreads();  // the previous step's readers of vb are done
     if (g == 0 && r0 >= k && r0 < k1)
 #pragma unroll
       for (int q = 0; q < R; ++q) vb[r0 + q - k] = SweepAcc<T>::pack(tr[q]);
@@ -1006,23 +1013,12 @@ __global__ void __launch_bounds__(SB / RowVec<T>::R * G, 512 / (SB / RowVec<T>::
         }
         fold_rows<T, R, CU>(acc, m, vb, idx, ok);
       }
-    if constexpr (G > 1) {
-      if (active)
+    if constexpr (G > 1)
 #pragma unroll
-        for (int q = 0; q < R; ++q) part[g][r0 - s0 + q] = acc[q].value();
-      __syncthreads();
-      if (g == 0 && active)
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-          double s = 0.0;
-#pragma unroll
-          for (int gg = 0; gg < G; ++gg) s += part[gg][r0 - s0 + q];
-          tr[q] -= s;
-        }
-    } else if (active) {
+      for (int q = 0; q < R; ++q) group_merge(acc[q], G);  // every lane of the warp takes part
+    if (active)
 #pragma unroll
       for (int q = 0; q < R; ++q) tr[q] -= acc[q].value();
-    }
   }
   if (g == 0)
 #pragma unroll
@@ -1033,37 +1029,70 @@ __global__ void __launch_bounds__(SB / RowVec<T>::R * G, 512 / (SB / RowVec<T>::
 // Backward chain, block upper with the stored block inverses: for the NB-blocks [k, k1) of
 // [s0, s1) in reverse,  x_k = D_k⁻¹ (z_k − M[k:k1, k1:s1] x[k1:s1]),  z = the tsave slots.
 // Writes x[elim[i]] for i < ne.  A thread owns R consecutive rows of the block and every G-th
-// column; the U loads and the D⁻¹ loads of a step are issued together, and the G partial sums
-// of a row meet in shared memory.
-template <typename T, int G>
-__global__ void __launch_bounds__(NB / RowVec<T>::R * G, 512 / (NB / RowVec<T>::R * G)) k_tri_bwd(const T* __restrict__ F,
-                                                                  const int64_t* __restrict__ f_off,
-                                                                  const double* __restrict__ tsave,
-                                                                  const int64_t* __restrict__ toff,
-                                                                  double* __restrict__ x,
-                                                                  const int32_t* __restrict__ elim,
-                                                                  const int64_t* __restrict__ elim_ptr,
-                                                                  const int32_t* __restrict__ f_ne, int64_t first,
-                                                                  int n, int s0, int s1) {
+// column; the U loads and the D⁻¹ loads of a step are issued together.  Column groups: 8 in
+// adjacent lanes (shuffle merges) times GH warps (merged through shared memory), G = 8·GH.
+template <typename T, int GH>
+__global__ void __launch_bounds__(32 * NB / RowVec<T>::R / 4 * GH, 512 / (32 * NB / RowVec<T>::R / 4 * GH)) k_tri_bwd(
+    const T* __restrict__ F, const int64_t* __restrict__ f_off, const double* __restrict__ tsave,
+    const int64_t* __restrict__ toff, double* __restrict__ x, const int32_t* __restrict__ elim,
+    const int64_t* __restrict__ elim_ptr, const int32_t* __restrict__ f_ne, int64_t first, int n, int s0, int s1) {
   using V = typename SweepAcc<T>::V;
   using VT = typename RowVec<T>::type;
-  constexpr int R = RowVec<T>::R, RQ = NB / R, CU = 16, CD = NB / G;
-  __shared__ V xv[SB];
-  __shared__ double part[G][NB];
+  constexpr int R = RowVec<T>::R, RQ = NB / R;  // row quads of a block
+  constexpr int RQW = 4;                         // row quads per warp (lanes: 8 column groups x 4)
+  constexpr int WPG = RQ / RQW;                  // warps per column-group set
+  constexpr int G = 8 * GH, CU = 16, CD = (NB + G - 1) / G;
+  __shared__ V xv[SB];              // the solved x of this super-block (packed)
   __shared__ V rhs[NB];
+  __shared__ float2 part[GH][NB];   // cross-warp partial sums (float-float)
   const int64_t f = first + blockIdx.x;
   const T* M = F + f_off[f];
   const double* z = tsave + toff[f];
   const int ne = f_ne[f];
   const int32_t* el = elim + elim_ptr[f];
-  const int rq = threadIdx.x % RQ, g = threadIdx.x / RQ;
+  const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+  const int g = (lane % 8) + 8 * (w / WPG);             // column group
+  const int gh = w / WPG;
+  const int rq = (lane / 8) + RQW * (w % WPG);          // row quad
   const int i0 = R * rq;
   const int nblk = (s1 - s0 + NB - 1) / NB;
+  auto merge_rows = [&](SweepAcc<T> (&a)[R], double (&out)[R]) {
+    // 8 adjacent lanes by shuffles, then the GH warp sets through shared memory
+#pragma unroll
+    for (int q = 0; q < R; ++q) group_merge(a[q], 8);
+    if constexpr (GH == 1) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) out[q] = a[q].value();
+    } else {
+      if constexpr (sizeof(T) == 4) {
+        if (lane % 8 == 0)
+#pragma unroll
+          for (int q = 0; q < R; ++q) part[gh][i0 + q] = make_float2(a[q].hi, a[q].lo);
+      } else {
+        if (lane % 8 == 0)
+#pragma unroll
+          for (int q = 0; q < R; ++q) part[gh][i0 + q] = make_float2((float)a[q].value(), 0.0f);  // unused for FP64
+      }
+      __syncthreads();
+      SweepAcc<T> s[R];
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        if constexpr (sizeof(T) == 4) {
+#pragma unroll
+          for (int h = 0; h < GH; ++h) s[q].merge(part[h][i0 + q].x, part[h][i0 + q].y);
+          out[q] = s[q].value();
+        } else {
+          out[q] = a[q].value();
+        }
+      }
+    }
+  };
+  static_assert(sizeof(T) == 4 || GH == 1, "FP64 factors use one warp set of column groups");
   for (int bk = nblk - 1; bk >= 0; --bk) {
     const int k = s0 + bk * NB, k1 = min(k + NB, s1), kb = k1 - k;
     const bool live = i0 < kb;  // kb is a multiple of R
     const T* rows = M + k + i0;
-    // D⁻¹ columns of this thread (independent of the chain: loaded with the first U chunk)
+    // D⁻¹ columns of this thread (independent of the chain: loaded with the U loads)
     VT dm[CD];
     int didx[CD];
     bool dok[CD];
@@ -1091,33 +1120,21 @@ __global__ void __launch_bounds__(NB / RowVec<T>::R * G, 512 / (NB / RowVec<T>::
         }
         fold_rows<T, R, CU>(acc, m, xv, idx, ok);
       }
-    if (live)
-#pragma unroll
-      for (int q = 0; q < R; ++q) part[g][i0 + q] = acc[q].value();
-    __syncthreads();
+    double sum[R];
+    merge_rows(acc, sum);
     if (g == 0 && live)
 #pragma unroll
-      for (int q = 0; q < R; ++q) {
-        double s = 0.0;
-        for (int gg = 0; gg < G; ++gg) s += part[gg][i0 + q];
-        rhs[i0 + q] = SweepAcc<T>::pack(z[k + i0 + q] - s);
-      }
+      for (int q = 0; q < R; ++q) rhs[i0 + q] = SweepAcc<T>::pack(z[k + i0 + q] - sum[q]);
     __syncthreads();
     // (2) x_k = D⁻¹ r
     SweepAcc<T> a2[R];
-    if (live) {
-      fold_rows<T, R, CD>(a2, dm, rhs, didx, dok);
-#pragma unroll
-      for (int q = 0; q < R; ++q) part[g][i0 + q] = a2[q].value();
-    }
-    __syncthreads();
+    if (live) fold_rows<T, R, CD>(a2, dm, rhs, didx, dok);
+    merge_rows(a2, sum);
     if (g == 0 && live)
 #pragma unroll
       for (int q = 0; q < R; ++q) {
-        double s = 0.0;
-        for (int gg = 0; gg < G; ++gg) s += part[gg][i0 + q];
-        xv[k + i0 + q - s0] = SweepAcc<T>::pack(s);
-        if (k + i0 + q < ne) x[el[k + i0 + q]] = s;
+        xv[k + i0 + q - s0] = SweepAcc<T>::pack(sum[q]);
+        if (k + i0 + q < ne) x[el[k + i0 + q]] = sum[q];
       }
     __syncthreads();
   }
@@ -1832,7 +1849,7 @@ static int sweep_cols(const gbmhd_ctx* ctx, int64_t rows, int64_t ncols, int64_t
 // column groups of the chain kernels: FP64 factors (two rows per thread) use half as many,
 // so that a CTA keeps at most 512 threads
 #define TRI_G(k) (sizeof(T) == 4 ? (k) : 1)
-#define TRI_GB(k) (sizeof(T) == 4 ? (k) : (k) / 2)
+#define TRI_GH(k) (sizeof(T) == 4 ? (k) : 1)
 template <typename T>
 static int gemv_t_cols(const gbmhd_ctx* ctx, int cols, int cnt) {
   if (sizeof(T) != 4) return 1;
@@ -1925,11 +1942,11 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       const int s0 = sb * SB, s1 = std::min(E, s0 + SB);
       if (!tr) {
         if ((rc = rect((size_t)l, 1, s0, s1, s1, n, 1))) return rc;
-        constexpr int RQ = NB / RowVec<T>::R;
-        if (cnt >= ctx->num_sms)
-          { k_tri_bwd<T, TRI_GB(8)><<<cnt, RQ * TRI_GB(8), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+        constexpr int W1 = 32 * NB / RowVec<T>::R / 4;  // threads of one column-group set
+        if (cnt >= ctx->num_sms || sizeof(T) == 8)
+          { k_tri_bwd<T, 1><<<cnt, W1, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
         else
-          { k_tri_bwd<T, TRI_GB(32)><<<cnt, RQ * TRI_GB(32), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+          { k_tri_bwd<T, TRI_GH(4)><<<cnt, W1 * TRI_GH(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
       } else {
         if ((rc = rect_t((size_t)l, s1, n, s0, s1, 1))) return rc;
         { k_tri_bwd_t<T><<<cnt, TT_THREADS, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr,

@@ -233,24 +233,63 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
       return rx != ry ? rx < ry : x < y;
     });
   }
-  // levels by height; front ids level by level
-  int32_t nlev = T[0].height + 1;
-  std::vector<std::vector<int32_t>> bylev(nlev);
-  for (int64_t v = 0; v < nn; ++v) bylev[T[v].height].push_back((int32_t)v);
-  std::vector<int32_t> fid(nn);
+  // Levels: the fronts of one tree height, in groups of similar size.  A group's fronts share
+  // padded sizes E, B and n (the batched kernels need them uniform), so one height whose fronts
+  // differ widely in size (irregular 3-D meshes) is split: fronts sorted by size, a group grows
+  // while its padded storage stays within 25 % of the fronts' own (at most 8 groups per height).
+  // Groups of one height are independent (a front's boundary dofs are eliminated by its
+  // ancestors, which are higher), so their order does not matter.
+  const int32_t nheight = T[0].height + 1;
+  std::vector<std::vector<int32_t>> byh(nheight);
+  for (int64_t v = 0; v < nn; ++v) byh[T[v].height].push_back((int32_t)v);
+  auto pad8 = [](int64_t x) { return (x + 7) / 8 * 8; };
+  std::vector<std::vector<int32_t>> groups;
+  for (int32_t h = 0; h < nheight; ++h) {
+    std::vector<int32_t>& vs = byh[h];
+    std::stable_sort(vs.begin(), vs.end(), [&](int32_t x, int32_t y) {
+      return T[x].elim.size() + bnd[x].size() > T[y].elim.size() + bnd[y].size();
+    });
+    const int64_t total = (int64_t)vs.size();
+    std::vector<int32_t> cur;
+    int64_t E = 0, B = 0;
+    double own = 0.0;
+    int made = 0;
+    for (int32_t v : vs) {
+      const int64_t e = (int64_t)T[v].elim.size(), b = (int64_t)bnd[v].size();
+      const int64_t E2 = std::max(E, e), B2 = std::max(B, b);
+      const double own2 = own + (double)(e + b) * (double)(e + b);
+      const double padded2 = (double)(cur.size() + 1) * (double)(pad8(std::max<int64_t>(E2, 1)) + pad8(B2)) *
+                             (double)(pad8(std::max<int64_t>(E2, 1)) + pad8(B2));
+      if (!cur.empty() && made < 7 && padded2 > 1.25 * own2 && (int64_t)cur.size() * 16 >= total / 8) {
+        groups.push_back(cur);
+        ++made;
+        cur.clear();
+        E = B = 0;
+        own = 0.0;
+      }
+      cur.push_back(v);
+      E = std::max(E, e);
+      B = std::max(B, b);
+      own += (double)(e + b) * (double)(e + b);
+    }
+    if (!cur.empty()) groups.push_back(cur);
+  }
+  const int32_t nlev = (int32_t)groups.size();
+  std::vector<int32_t> fid(nn), level_of(nn);
   S.levels.resize(nlev);
   int64_t nf = 0, off = 0;
   for (int32_t l = 0; l < nlev; ++l) {
     MFLevel& L = S.levels[l];
     L.first = nf;
-    L.count = (int64_t)bylev[l].size();
-    for (int32_t v : bylev[l]) {
+    L.count = (int64_t)groups[l].size();
+    for (int32_t v : groups[l]) {
       L.E = std::max<int32_t>(L.E, (int32_t)T[v].elim.size());
       L.B = std::max<int32_t>(L.B, (int32_t)bnd[v].size());
       fid[v] = (int32_t)nf++;
+      level_of[v] = l;
     }
-    // padded to multiples of 8 so that every front column starts 32-byte aligned: cuBLAS
-    // then runs its tensor-core kernels (an odd leading dimension falls back to SIMT ones)
+    // padded to multiples of 8: every front column starts 32-byte aligned, and the sweeps'
+    // 16-byte vector loads and TMA boxes stay aligned
     L.E = (std::max(L.E, 1) + 7) / 8 * 8;
     L.B = (L.B + 7) / 8 * 8;
     L.n = L.E + L.B;
@@ -263,7 +302,7 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
   S.elim_ptr.assign(nf + 1, 0); S.bnd_ptr.assign(nf + 1, 0);
   for (int64_t v = 0; v < nn; ++v) {
     const int32_t f = fid[v];
-    const int l = T[v].height;
+    const int l = level_of[v];
     S.f_ne[f] = (int32_t)T[v].elim.size();
     S.f_nb[f] = (int32_t)bnd[v].size();
     S.f_level[f] = l;

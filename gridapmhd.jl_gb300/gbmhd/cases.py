@@ -48,13 +48,16 @@ def gpu_context(mesh, dm, params):
                    [dm.dir_values.get(f) for f in ("u", "p", "j", "phi")], params)
 
 
-def expansion_case(n_up=3, n_down=6, n_y_in=3, n_y_out=3, n_z=3, Ha=20.0, Re=10.0, ratio=4.0, convection=2):
+def expansion_case(n_up=3, n_down=6, n_y_in=3, n_y_out=3, n_z=3, Ha=20.0, Re=10.0, ratio=4.0, convection=2,
+                   L_up=1.0, L_down=2.0, grading=2.0, thin_wall=None):
     """Sudden expansion in MHD scaling (α=1/N, β=1/Ha², γ=1; src/Applications/expansion.jl:113-123):
-    parabolic inlet velocity, u and j Dirichlet on walls/inlet, j Dirichlet on the outlet,
-    natural (∇p-free) outlet for u, B=(0,1,0)."""
+    parabolic inlet velocity, u Dirichlet on walls/inlet, natural (∇p-free) outlet for u,
+    B=(0,1,0).  Walls: j Dirichlet on wall, inlet and outlet (insulating, :150-159), or with
+    thin_wall=(τ, cw) the thin-wall law on "wall" and j Dirichlet on inlet and outlet only
+    (:160-167)."""
     from .mesh import expansion_mesh
     mesh = expansion_mesh(n_up=n_up, n_down=n_down, n_y_in=n_y_in, n_y_out=n_y_out, n_z=n_z, ratio=ratio,
-                          L_up=1.0, L_down=2.0, grading=2.0)
+                          L_up=L_up, L_down=L_down, grading=grading)
     h = mesh.meta["h_in"]
     w = mesh.meta["width"]
     H = mesh.meta["H"]
@@ -69,8 +72,16 @@ def expansion_case(n_up=3, n_down=6, n_y_in=3, n_y_out=3, n_z=3, Ha=20.0, Re=10.
         inlet = P[:, 0] < -mesh.meta["L_up"] + 1e-9
         out[inlet, 0] = scale * prof[inlet]
         return out
-    dm = build_dofmap(mesh, ["wall", "inlet"], ["wall", "inlet", "outlet"], u_values=u_in)
+    jtags = ["wall", "inlet", "outlet"] if thin_wall is None else ["inlet", "outlet"]
+    dm = build_dofmap(mesh, ["wall", "inlet"], jtags, u_values=u_in)
     N = Ha ** 2 / Re
     params = dict(alpha=1.0 / N, beta=1.0 / Ha ** 2, gamma=1.0, sigma=1.0, B=(0, 1, 0), f=(0.0, 0.0, 0.0),
                   zeta_u=0.0, zeta_j=0.0, convection=convection, facets=None)
+    if thin_wall is not None:
+        tau, cw = thin_wall
+        bc, bf, bt = mesh.boundary_faces()
+        sel = bt == mesh.tag_names.index("wall")
+        n = int(sel.sum())
+        params["facets"] = dict(cell=bc[sel].astype(np.int32), lface=bf[sel].astype(np.int8), tau=np.full(n, tau),
+                                cw=np.full(n, cw), jw=np.zeros(n), phi0=None)
     return mesh, dm, params

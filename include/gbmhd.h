@@ -242,6 +242,9 @@ int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double*
  *                                   that has run GBMHD_STAG_ITERS iterations (default 100) with
  *                                   its relative residual still above GBMHD_STAG_REL (default
  *                                   0.5) triggers the refactorization / FP64 fallback
+ *   GBMHD_SWEEP_GRAPHS              0: launch the kernels of each preconditioner application one
+ *                                   by one instead of replaying them as a CUDA graph (for per-kernel
+ *                                   profiling; read when a context first factors; default 1)
  *   GBMHD_SWEEP_WAIT_LIMIT          spin limit of the TMA solve sweeps' mbarrier waits, read
  *                                   when a context first factors (default 4,194,304); a wait
  *                                   that runs out drains its copies and makes the Newton step
