@@ -954,6 +954,47 @@ __device__ __forceinline__ void group_merge(SweepAcc<double>& a, int width) {
   for (int o = width / 2; o > 0; o >>= 1) a.a += __shfl_xor_sync(0xffffffffu, a.a, o);
 }
 
+// An accumulator's value in the packed vector format (float-float, or FP64)
+__device__ __forceinline__ float2 acc_packed(const SweepAcc<float>& a) { return make_float2(a.hi, a.lo); }
+__device__ __forceinline__ double acc_packed(const SweepAcc<double>& a) { return a.a; }
+
+// Packed vector values (float-float, or FP64): p − a, and the FP64 value
+__device__ __forceinline__ float2 vsub(float2 p, const SweepAcc<float>& a) {
+  SweepAcc<float> s;
+  s.hi = p.x;
+  s.lo = p.y;
+  s.merge(-a.hi, -a.lo);
+  return make_float2(s.hi, s.lo);
+}
+__device__ __forceinline__ double vsub(double p, const SweepAcc<double>& a) { return p - a.a; }
+__device__ __forceinline__ double vto(float2 p) { return (double)p.x + (double)p.y; }
+__device__ __forceinline__ double vto(double p) { return p; }
+
+// Vector values inside the chain kernels: float-float for FP32 factors (FP32 arithmetic in
+// every step; FP64 only where a value is read from or written to the FP64 vectors), FP64 for
+// FP64 factors.
+template <typename T>
+struct ChainVal;
+template <>
+struct ChainVal<float> {
+  SweepAcc<float> v;
+  __device__ void set(double d) {
+    v.hi = (float)d;
+    v.lo = (float)(d - (double)v.hi);
+  }
+  __device__ void sub(const SweepAcc<float>& a) { v.merge(-a.hi, -a.lo); }
+  __device__ float2 packed() const { return make_float2(v.hi, v.lo); }
+  __device__ double value() const { return v.value(); }
+};
+template <>
+struct ChainVal<double> {
+  double v = 0.0;
+  __device__ void set(double d) { v = d; }
+  __device__ void sub(const SweepAcc<double>& a) { v -= a.a; }
+  __device__ double packed() const { return v; }
+  __device__ double value() const { return v; }
+};
+
 // Forward chain, unit lower: for the NB-blocks [k, k1) of [s0, s1) in order,
 //   t[k1:s1] −= M[k1:s1, k:k1] t[k:k1]      (t = the front's tsave slots, in place).
 // A thread owns R consecutive rows (16-byte loads along the column-major front) and every
@@ -983,18 +1024,18 @@ __global__ void __launch_bounds__(SB / RowVec<T>::R * G, 512 / (SB / RowVec<T>::
   if (gather)
     for (int i = threadIdx.x; i < E; i += blockDim.x)
       if (i < s0 || i >= s1) t[i] = i < ne ? b[el[i]] : 0.0;
-  double tr[R];
+  ChainVal<T> tr[R];
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     const int r = r0 + q;
-    tr[q] = r < s1 ? (gather ? (r < ne ? b[el[r]] : 0.0) : t[r]) : 0.0;
+    tr[q].set(r < s1 ? (gather ? (r < ne ? b[el[r]] : 0.0) : t[r]) : 0.0);
   }
   for (int k = s0; k < s1; k += NB) {
     const int k1 = min(k + NB, s1);
     __syncthreads();  // the previous step's readers of vb are done
     if (g == 0 && r0 >= k && r0 < k1)
 #pragma unroll
-      for (int q = 0; q < R; ++q) vb[r0 + q - k] = SweepAcc<T>::pack(tr[q]);
+      for (int q = 0; q < R; ++q) vb[r0 + q - k] = tr[q].packed();
     __syncthreads();
     const bool active = r0 >= k1 && r0 < s1;  // k1 and s1 are multiples of R
     SweepAcc<T> acc[R];
@@ -1018,12 +1059,12 @@ __global__ void __launch_bounds__(SB / RowVec<T>::R * G, 512 / (SB / RowVec<T>::
       for (int q = 0; q < R; ++q) group_merge(acc[q], G);  // every lane of the warp takes part
     if (active)
 #pragma unroll
-      for (int q = 0; q < R; ++q) tr[q] -= acc[q].value();
+      for (int q = 0; q < R; ++q) tr[q].sub(acc[q]);
   }
   if (g == 0)
 #pragma unroll
     for (int q = 0; q < R; ++q)
-      if (r0 + q < s1) t[r0 + q] = tr[q];
+      if (r0 + q < s1) t[r0 + q] = tr[q].value();
 }
 
 // Backward chain, block upper with the stored block inverses: for the NB-blocks [k, k1) of
@@ -1056,34 +1097,22 @@ __global__ void __launch_bounds__(32 * NB / RowVec<T>::R / 4 * GH, 512 / (32 * N
   const int rq = (lane / 8) + RQW * (w % WPG);          // row quad
   const int i0 = R * rq;
   const int nblk = (s1 - s0 + NB - 1) / NB;
-  auto merge_rows = [&](SweepAcc<T> (&a)[R], double (&out)[R]) {
-    // 8 adjacent lanes by shuffles, then the GH warp sets through shared memory
+  auto merge_rows = [&](SweepAcc<T> (&a)[R]) {
+    // 8 adjacent lanes by shuffles, then the GH warp sets through shared memory; the row sums
+    // end in a (all lanes of a column-group set hold them)
 #pragma unroll
     for (int q = 0; q < R; ++q) group_merge(a[q], 8);
-    if constexpr (GH == 1) {
+    if constexpr (GH > 1 && sizeof(T) == 4) {
+      if (lane % 8 == 0)
 #pragma unroll
-      for (int q = 0; q < R; ++q) out[q] = a[q].value();
-    } else {
-      if constexpr (sizeof(T) == 4) {
-        if (lane % 8 == 0)
-#pragma unroll
-          for (int q = 0; q < R; ++q) part[gh][i0 + q] = make_float2(a[q].hi, a[q].lo);
-      } else {
-        if (lane % 8 == 0)
-#pragma unroll
-          for (int q = 0; q < R; ++q) part[gh][i0 + q] = make_float2((float)a[q].value(), 0.0f);  // unused for FP64
-      }
+        for (int q = 0; q < R; ++q) part[gh][i0 + q] = make_float2(a[q].hi, a[q].lo);
       __syncthreads();
-      SweepAcc<T> s[R];
 #pragma unroll
       for (int q = 0; q < R; ++q) {
-        if constexpr (sizeof(T) == 4) {
+        SweepAcc<T> s;
 #pragma unroll
-          for (int h = 0; h < GH; ++h) s[q].merge(part[h][i0 + q].x, part[h][i0 + q].y);
-          out[q] = s[q].value();
-        } else {
-          out[q] = a[q].value();
-        }
+        for (int h = 0; h < GH; ++h) s.merge(part[h][i0 + q].x, part[h][i0 + q].y);
+        a[q] = s;
       }
     }
   };
@@ -1120,21 +1149,25 @@ __global__ void __launch_bounds__(32 * NB / RowVec<T>::R / 4 * GH, 512 / (32 * N
         }
         fold_rows<T, R, CU>(acc, m, xv, idx, ok);
       }
-    double sum[R];
-    merge_rows(acc, sum);
+    merge_rows(acc);
     if (g == 0 && live)
 #pragma unroll
-      for (int q = 0; q < R; ++q) rhs[i0 + q] = SweepAcc<T>::pack(z[k + i0 + q] - sum[q]);
+      for (int q = 0; q < R; ++q) {
+        ChainVal<T> r;
+        r.set(z[k + i0 + q]);
+        r.sub(acc[q]);
+        rhs[i0 + q] = r.packed();
+      }
     __syncthreads();
     // (2) x_k = D⁻¹ r
     SweepAcc<T> a2[R];
     if (live) fold_rows<T, R, CD>(a2, dm, rhs, didx, dok);
-    merge_rows(a2, sum);
+    merge_rows(a2);
     if (g == 0 && live)
 #pragma unroll
       for (int q = 0; q < R; ++q) {
-        xv[k + i0 + q - s0] = SweepAcc<T>::pack(sum[q]);
-        if (k + i0 + q < ne) x[el[k + i0 + q]] = sum[q];
+        xv[k + i0 + q - s0] = acc_packed(a2[q]);
+        if (k + i0 + q < ne) x[el[k + i0 + q]] = a2[q].value();
       }
     __syncthreads();
   }
@@ -1158,7 +1191,7 @@ __global__ void __launch_bounds__(TT_THREADS) k_tri_fwd_t(const T* __restrict__ 
   using VT = typename RowVec<T>::type;
   constexpr int R = RowVec<T>::R, LV = NB / 8 / R;  // vector loads per lane and column
   constexpr int NP = SB / (TT_THREADS / 8);          // passes of 64 columns over a super-block
-  __shared__ double tt[SB];
+  __shared__ V tt[SB];  // packed (FP32 arithmetic on float-float for FP32 factors)
   __shared__ V yb[NB];
   const int64_t f = first + blockIdx.x;
   const T* M = F + f_off[f];
@@ -1169,11 +1202,11 @@ __global__ void __launch_bounds__(TT_THREADS) k_tri_fwd_t(const T* __restrict__ 
   if (gather) {
     for (int i = threadIdx.x; i < E; i += blockDim.x) {
       const double v = i < ne ? b[el[i]] : 0.0;
-      if (i >= s0 && i < s1) tt[i - s0] = v;
+      if (i >= s0 && i < s1) tt[i - s0] = SweepAcc<T>::pack(v);
       else t[i] = v;
     }
   } else {
-    for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) tt[i] = t[s0 + i];
+    for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) tt[i] = SweepAcc<T>::pack(t[s0 + i]);
   }
   __syncthreads();
   for (int k = s0; k < s1; k += NB) {
@@ -1189,16 +1222,15 @@ __global__ void __launch_bounds__(TT_THREADS) k_tri_fwd_t(const T* __restrict__ 
           if (r < kb) {
             const VT m = *reinterpret_cast<const VT*>(col + r);
 #pragma unroll
-            for (int q = 0; q < R; ++q) acc.add(reinterpret_cast<const T*>(&m)[q], SweepAcc<T>::pack(tt[k - s0 + r + q]));
+            for (int q = 0; q < R; ++q) acc.add(reinterpret_cast<const T*>(&m)[q], tt[k - s0 + r + q]);
           }
         }
       }
       acc.warp_reduce8();
       __syncthreads();  // every lane has read tt[k..k1)
       if (j == 0 && cs < kb) {
-        const double y = acc.value();
-        tt[k - s0 + cs] = y;
-        yb[cs] = SweepAcc<T>::pack(y);
+        tt[k - s0 + cs] = acc_packed(acc);
+        yb[cs] = acc_packed(acc);
       }
       __syncthreads();
     }
@@ -1225,11 +1257,11 @@ __global__ void __launch_bounds__(TT_THREADS) k_tri_fwd_t(const T* __restrict__ 
           for (int q = 0; q < R; ++q) acc.add(reinterpret_cast<const T*>(&m[p][u])[q], yb[r + q]);
       }
       acc.warp_reduce8();
-      if (j == 0 && c < s1) tt[c - s0] = dsub<T>(tt[c - s0], acc);
+      if (j == 0 && c < s1) tt[c - s0] = vsub(tt[c - s0], acc);
     }
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) t[s0 + i] = tt[i];
+  for (int i = threadIdx.x; i < s1 - s0; i += blockDim.x) t[s0 + i] = vto(tt[i]);
 }
 
 // Transposed backward chain (Lᵀ: unit upper): for the NB-blocks [k, k1) of [s0, s1) in
@@ -1276,9 +1308,9 @@ __global__ void __launch_bounds__(TT_THREADS) k_tri_bwd_t(const T* __restrict__ 
     }
     acc.warp_reduce8();
     if (j == 0 && cs < kb) {
-      const double v = dsub<T>(z[k + cs], acc);
-      xv[k + cs - s0] = SweepAcc<T>::pack(v);
-      if (k + cs < ne) x[el[k + cs]] = v;
+      const V v = vsub(SweepAcc<T>::pack(z[k + cs]), acc);
+      xv[k + cs - s0] = v;
+      if (k + cs < ne) x[el[k + cs]] = vto(v);
     }
     __syncthreads();
   }

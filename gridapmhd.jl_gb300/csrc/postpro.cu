@@ -224,3 +224,122 @@ extern "C" int gbmhd_hunt_errors(gbmhd_ctx* ctx, const double* x_free, const gbm
   for (int k = 0; k < 9; ++k) out[k] = std::sqrt(std::max(0.0, sum[k]));
   return 0;
 }
+
+// ---------------------------------------------------------------- fields at the Q2 nodes (VTK)
+// The solution at the 27 nodes ξ ∈ {0, ½, 1}³ of every cell, for a field file of order 2 like
+// the post-processing of hunt() writes (src/Applications/hunt.jl:263-273): per node the
+// physical point, u_h, p_h, j_h (contravariant Piola map), φ_h, div u_h and div j_h.  u_h is
+// nodal (its dof values), the others are evaluated from the closed-form reference bases.
+namespace gbmhd {
+namespace {
+
+constexpr int NODE_FIELDS = 13;
+
+__device__ __forceinline__ double l2v(int a, double t) {
+  return a == 0 ? (2 * t - 1) * (t - 1) : (a == 1 ? 4 * t * (1 - t) : t * (2 * t - 1));
+}
+__device__ __forceinline__ double l2d(int a, double t) { return a == 0 ? 4 * t - 3 : (a == 1 ? 4 - 8 * t : 4 * t - 1); }
+__device__ __forceinline__ double l1v(int a, double t) { return a ? t : 1 - t; }
+__device__ __forceinline__ double l1d(int a) { return a ? 1.0 : -1.0; }
+
+__global__ void __launch_bounds__(32) k_node_fields(int64_t ncells, const double* __restrict__ cellX,
+                                                    const int32_t* __restrict__ gidx,
+                                                    const uint64_t* __restrict__ sign,
+                                                    const double* __restrict__ xfull, double* __restrict__ out) {
+  __shared__ double X[24], v[ND];
+  __shared__ unsigned long long sg;
+  const int t = threadIdx.x;
+  for (int64_t cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
+    __syncwarp();
+    if (t < 24) X[t] = cellX[cell * 24 + t];
+    for (int a = t; a < ND; a += 32) v[a] = xfull[gidx[cell * ND + a]];
+    if (t == 0) sg = sign ? sign[cell] : 0ull;
+    __syncwarp();
+    if (t < 27) {
+      const int na = t % 3, nb = (t / 3) % 3, nc = t / 9;
+      const double xi[3] = {0.5 * na, 0.5 * nb, 0.5 * nc};
+      // trilinear geometry
+      double x[3] = {0, 0, 0}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      for (int vv = 0; vv < 8; ++vv) {
+        const int a = vv & 1, b = (vv >> 1) & 1, c = (vv >> 2) & 1;
+        const double f = l1v(a, xi[0]) * l1v(b, xi[1]) * l1v(c, xi[2]);
+        const double g[3] = {l1d(a) * l1v(b, xi[1]) * l1v(c, xi[2]), l1v(a, xi[0]) * l1d(b) * l1v(c, xi[2]),
+                             l1v(a, xi[0]) * l1v(b, xi[1]) * l1d(c)};
+        for (int i = 0; i < 3; ++i) {
+          x[i] += X[3 * vv + i] * f;
+          for (int e = 0; e < 3; ++e) J[i][e] += X[3 * vv + i] * g[e];
+        }
+      }
+      const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      const double id = 1.0 / det;
+      double Ji[3][3];  // Ji[e][i] = ∂ξ_e/∂x_i
+      Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * id;
+      Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+      Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+      Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+      Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+      Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+      Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * id;
+      Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+      Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+      // div u_h: Σ_n Σ_c u_{c,n} ∂_c N_n
+      double divu = 0.0;
+      for (int n = 0; n < 27; ++n) {
+        const int a = n % 3, b = (n / 3) % 3, c = n / 9;
+        const double g[3] = {l2d(a, xi[0]) * l2v(b, xi[1]) * l2v(c, xi[2]),
+                             l2v(a, xi[0]) * l2d(b, xi[1]) * l2v(c, xi[2]),
+                             l2v(a, xi[0]) * l2v(b, xi[1]) * l2d(c, xi[2])};
+        for (int cc = 0; cc < 3; ++cc)
+          divu += v[OU + cc * 27 + n] * (Ji[0][cc] * g[0] + Ji[1][cc] * g[1] + Ji[2][cc] * g[2]);
+      }
+      // p_h (P1: 1 − ξ1 − ξ2 − ξ3, ξ1, ξ2, ξ3) and φ_h (Q1 at the vertices)
+      const double p = v[OP] * (1 - xi[0] - xi[1] - xi[2]) + v[OP + 1] * xi[0] + v[OP + 2] * xi[1] + v[OP + 3] * xi[2];
+      double phi = 0.0;
+      for (int vv = 0; vv < 8; ++vv)
+        phi += v[OPHI + vv] * l1v(vv & 1, xi[0]) * l1v((vv >> 1) & 1, xi[1]) * l1v((vv >> 2) & 1, xi[2]);
+      // j_h = J ĵ / det J, div j_h = div ĵ / det J (RT: b = d·12 + q + 3(l1 + 2 l2))
+      double ja[3] = {0, 0, 0}, dj = 0.0;
+      for (int b = 0; b < 36; ++b) {
+        const int d = b / 12, r = b % 12, q = r % 3, la = (r / 3) % 2, lb = (r / 3) / 2;
+        const int o1 = d == 0 ? 1 : 0, o2 = d == 2 ? 1 : 2;
+        const double sgb = ((sg >> b) & 1ull) ? -1.0 : 1.0;
+        const double w = sgb * v[OJ + b] * l1v(la, xi[o1]) * l1v(lb, xi[o2]);
+        ja[d] += w * l2v(q, xi[d]);
+        dj += w * l2d(q, xi[d]);
+      }
+      double* o = out + ((size_t)cell * 27 + t) * NODE_FIELDS;
+      o[0] = x[0]; o[1] = x[1]; o[2] = x[2];
+      o[3] = v[OU + na + 3 * nb + 9 * nc]; o[4] = v[OU + 27 + na + 3 * nb + 9 * nc]; o[5] = v[OU + 54 + na + 3 * nb + 9 * nc];
+      o[6] = p;
+      for (int i = 0; i < 3; ++i) o[7 + i] = (J[i][0] * ja[0] + J[i][1] * ja[1] + J[i][2] * ja[2]) * id;
+      o[10] = phi;
+      o[11] = divu;
+      o[12] = dj * id;
+    }
+  }
+}
+
+}  // namespace
+}  // namespace gbmhd
+
+extern "C" int gbmhd_node_fields(gbmhd_ctx* ctx, const double* x_free, double* out) {
+  if (!ctx) return -1;
+  if (!x_free || !out) { ctx->err = "node_fields: NULL argument"; return -1; }
+  const size_t nout = (size_t)ctx->ncells * 27 * gbmhd::NODE_FIELDS;
+  double* d_out = nullptr;
+  GB_CUDA(cudaMallocAsync(&d_out, sizeof(double) * std::max<size_t>(nout, 1), ctx->stream));
+  GB_CUDA(cudaMemcpyAsync(ctx->d_xfull, x_free, sizeof(double) * ctx->ndofs, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->ncells > 0) {
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(ctx->ncells, (int64_t)ctx->num_sms * 64));
+    gbmhd::k_node_fields<<<(unsigned)grid, 32, 0, ctx->stream>>>(ctx->ncells, ctx->d_cellX, ctx->d_gidx, ctx->d_sign,
+                                                                ctx->d_xfull, d_out);
+    gbmhd::count_launch();
+    GB_CUDA(cudaGetLastError());
+  }
+  GB_CUDA(cudaMemcpyAsync(out, d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, ctx->stream));
+  GB_CUDA(cudaFreeAsync(d_out, ctx->stream));
+  GB_CUDA(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}

@@ -131,8 +131,17 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
     const float* src = isA ? Ab + gi : Bb + (int64_t)gi * ldb;
     const int64_t stride = isA ? lda : 1;
     const int kn = live ? min(KH, k - kb0) : 0;
+    if (!isA && kn == KH && (reinterpret_cast<uintptr_t>(src + kb0) & 15) == 0) {
+      // a row of Bᵀ is K-contiguous: sixteen 16-byte loads
 #pragma unroll
-    for (int u = 0; u < KH; ++u) v[u] = u < kn ? src[(int64_t)(kb0 + u) * stride] : 0.0f;
+      for (int u = 0; u < KH / 4; ++u) {
+        const float4 q = *reinterpret_cast<const float4*>(src + kb0 + 4 * u);
+        v[4 * u] = q.x; v[4 * u + 1] = q.y; v[4 * u + 2] = q.z; v[4 * u + 3] = q.w;
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < KH; ++u) v[u] = u < kn ? src[(int64_t)(kb0 + u) * stride] : 0.0f;
+    }
 #pragma unroll
     for (int kc = 0; kc < KH / 8; ++kc) {
       // core matrix (row group row/8, K group kc): kc·(128·16) + (row/8)·128 + (row%8)·16

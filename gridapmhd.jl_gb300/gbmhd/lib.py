@@ -23,7 +23,7 @@ GBMHD_PC_BADIA2024 = 1
 
 SYMBOLS = ["gbmhd_version", "gbmhd_create", "gbmhd_set_params", "gbmhd_sizes", "gbmhd_assemble",
            "gbmhd_assemble_device", "gbmhd_get_csr", "gbmhd_newton_solve", "gbmhd_newton_solve_device",
-           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_sweep_stats", "gbmhd_hunt_errors", "gbmhd_diag_tc_gemm", "gbmhd_diag_pc_compare", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
+           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_sweep_stats", "gbmhd_hunt_errors", "gbmhd_diag_tc_gemm", "gbmhd_diag_pc_compare", "gbmhd_node_fields", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -121,6 +121,7 @@ def load(path: Optional[str] = None):
                                       C.c_void_p, C.c_int32, C.c_int64, C.c_float, C.c_void_p, C.c_int32,
                                       C.c_int64, C.c_int32, C.POINTER(C.c_int32)]
     L.gbmhd_diag_pc_compare.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, _dp]
+    L.gbmhd_node_fields.argtypes = [C.c_void_p, _dp, _dp]
     L.gbmhd_hunt_errors.argtypes = [C.c_void_p, _dp, C.POINTER(HuntAnalytic), _dp]
     L.gbmhd_counters.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.gbmhd_destroy.argtypes = [C.c_void_p]
@@ -249,6 +250,13 @@ class Context:
         self._check(self.L.gbmhd_diag_uj_solve_error(self.h, C.c_void_p(d_state), int(precision), C.byref(e)),
                     "gbmhd_diag_uj_solve_error")
         return e.value
+
+    def node_fields(self, x: np.ndarray) -> np.ndarray:
+        """(ncells, 27, 13): point, u, p, j, φ, div u, div j at the Q2 nodes (gbmhd_node_fields)."""
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.empty((self.ncells, 27, 13))
+        self._check(self.L.gbmhd_node_fields(self.h, _ptr(x), _ptr(out)), "gbmhd_node_fields")
+        return out
 
     def pc_compare(self, d_state: int, transpose=False) -> float:
         """‖y32 − y64‖/‖y64‖ for y = P⁻¹b (P⁻ᵀb), FP32 against FP64 factors (gbmhd_diag_pc_compare)."""

@@ -283,13 +283,16 @@ def hunt(*, nc=(4, 4), ν=1.0, ρ=1.0, σ=1.0, B=(0.0, 10.0, 0.0), f=(0.0, 0.0, 
          u0=1.0, B0=None, tw=0.0, order=2, nsums=10, title="hunt", path=".", debug=False, res_assemble=False,
          jac_assemble=False, solve=True, solver="gb300", formulation="cfd", initial_value="zero",
          convection="newton", BL_adapted=True, kmap_x=1, kmap_y=1, nz=3, Lz=0.1, map_beta=None, cw=0.0, τ=100.0,
-         write=False, **kw) -> Dict[str, Any]:
+         write=False, vtk=False, **kw) -> Dict[str, Any]:
     """``hunt(; kwargs...)`` (src/Applications/hunt.jl:1-304) on the GPU.
 
     Extra keywords for the duct configurations of the GPU benchmark: ``nz``,
     ``Lz`` (axial cells and length; the reference hard-codes 3 and 0.1),
     ``map_beta`` (tanh stretching instead of the Smolentsev/power maps) and
     ``cw``/``τ`` (thin-wall law on the Hartmann walls, src/weakforms.jl:721-733).
+    With ``vtk=True`` the fields uh, ph, jh, phi, div_uh and div_jh are written to
+    ``<path>/<title>.vtu`` at order 2, as the reference does (src/Applications/hunt.jl:263-273;
+    the fields are evaluated on the device, gbmhd_node_fields, and carry the solved units).
     Returns the ``info`` dict the reference saves to BSON."""
     if kw:
         raise TypeError(f"unexpected keyword(s) {sorted(kw)}")
@@ -340,6 +343,13 @@ def hunt(*, nc=(4, 4), ν=1.0, ρ=1.0, σ=1.0, B=(0.0, 10.0, 0.0), f=(0.0, 0.0, 
                 ndofs_j=dm.nfree["j"], ndofs_φ=dm.nfree["phi"], ndofs=dm.ndofs, Re=Re, Ha=Ha, nsums=nsums,
                 kmap=[kmap_x, kmap_y], title=title)
     info["xh"] = xh
+    if vtk:
+        from .vtk import write_vtu
+        tv = time.perf_counter()
+        os.makedirs(path, exist_ok=True)
+        info["vtk_file"] = write_vtu(os.path.join(path, f"{title}.vtu"),
+                                     full["_context"].node_fields(xh.free_values))
+        info["time_vtk"] = time.perf_counter() - tv
     if write:
         os.makedirs(path, exist_ok=True)
         with open(os.path.join(path, f"{title}.json"), "w") as fh:

@@ -227,6 +227,13 @@ int gbmhd_diag_uj_solve_error(gbmhd_ctx* ctx, const double* d_state, int32_t pre
  * of a cell do not change with length_scale, their gradients scale by 1/length_scale. */
 int gbmhd_hunt_errors(gbmhd_ctx* ctx, const double* x_free, const gbmhd_hunt_analytic* a, double* out);
 
+/* The solution at the 27 Q2 nodes ξ ∈ {0, ½, 1}³ of every cell (node n = a + 3b + 9c), on the
+ * device, for field output of order 2 as hunt(..., vtk=true) writes it
+ * (src/Applications/hunt.jl:263-273): out [ncells][27][13] receives per node the physical
+ * point (3), u_h (3), p_h, j_h (3, contravariant Piola map), φ_h, div u_h and div j_h.
+ * x_free is the host free vector [ndofs]; the Dirichlet values are the context's. */
+int gbmhd_node_fields(gbmhd_ctx* ctx, const double* x_free, double* out);
+
 /* Diagnostics: multifrontal solves (preconditioner applications) timed with CUDA events
  * on the context stream since the last call, their total device time in seconds, and
  * the factor bytes one solve reads (padding excluded); resets the counters. */
