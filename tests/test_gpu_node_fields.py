@@ -27,12 +27,15 @@ def test_node_fields_match_the_oracle_bases(gpu_lib):
         for n in range(27):
             xi = np.array([0.5 * (n % 3), 0.5 * ((n // 3) % 3), 0.5 * (n // 9)])
             q2, rt, rtdiv, p1, q1 = _ref(xi)
-            # trilinear map and its Jacobian by central differences of the Q1 values
+            # trilinear map and its Jacobian (closed-form gradients of the Q1 vertex functions)
             pt = q1 @ X[c]
             J = np.zeros((3, 3))
-            for e in range(3):
-                d = np.zeros(3); d[e] = 1e-6
-                J[:, e] = (_ref(xi + d)[4] @ X[c] - _ref(xi - d)[4] @ X[c]) / 2e-6
+            for v in range(8):
+                a, b, cc = v & 1, (v >> 1) & 1, (v >> 2) & 1
+                L = [(1 - xi[0], xi[0]), (1 - xi[1], xi[1]), (1 - xi[2], xi[2])]
+                d = (-1.0, 1.0)
+                g = np.array([d[a] * L[1][b] * L[2][cc], L[0][a] * d[b] * L[2][cc], L[0][a] * L[1][b] * d[cc]])
+                J += np.outer(X[c, v], g)
             det = np.linalg.det(J)
             u = np.array([xc[c, 27 * k:27 * k + 27] @ q2 for k in range(3)])
             p = xc[c, 81:85] @ p1
@@ -43,5 +46,6 @@ def test_node_fields_match_the_oracle_bases(gpu_lib):
             assert np.allclose(o[0:3], pt, atol=1e-12)
             assert np.allclose(o[3:6], u, atol=1e-12)
             assert abs(o[6] - p) <= 1e-12 and abs(o[10] - phi) <= 1e-12
-            assert np.allclose(o[7:10], j, rtol=1e-7, atol=1e-9)   # J by finite differences
-            assert abs(o[12] - divj) <= 1e-7 * max(1.0, abs(divj))
+            scale = max(1.0, np.abs(j).max())
+            assert np.abs(o[7:10] - j).max() <= 1e-12 * scale, (o[7:10], j)
+            assert abs(o[12] - divj) <= 1e-12 * max(1.0, abs(divj))
