@@ -57,6 +57,8 @@ struct MFNumeric {
   std::vector<CUtensorMap> maps;
   std::vector<int> map_rows;      // row tile of each map
   std::vector<char> map_ok;
+  std::vector<CUtensorMap> cmaps;  // per level: NB x NB boxes of the substitution chains
+  std::vector<char> cmap_ok;
   const void* maps_base = nullptr;
   float2* vpk = nullptr;            // packed vector segments of one level (transposed GEMVs)
   bool scaled = false;              // factors are those of Dr A Dc (monolithic)
@@ -1568,6 +1570,237 @@ __global__ void __launch_bounds__(TS_THREADS) k_rect_tma(const __grid_constant__
   if (i0 + 1 < r1) front_sub(i0 + 1, E, nb, t, b, bd, a1.value());
 }
 
+// ---- substitution chains with TMA-staged blocks (FP32 factors)
+// Every NB x NB block a chain reads is one TMA box (NB rows x NB columns of one front, 16 KB),
+// copied into a ring of NSLOT shared-memory slots by thread 0 ahead of the step that uses
+// it; a step waits only for its own blocks, and the ring is refilled after each step.  A step
+// reads at most nb ≤ NSLOT blocks (checked on the host), so the ring never waits on itself.
+// Thread layout: R = 4 consecutive rows of the super-block (one 16-byte shared-memory load
+// per column) times G column groups; the G lanes of a row quad are LPR = 32 / G lanes apart
+// in one warp (conflict-free shared-memory rows, xor-shuffle merges).  Waits are bounded: one
+// that runs out makes the CTA wait (with the full limit) for its copies in flight, set the
+// error flag and return.
+constexpr int CH_BOX_BYTES = NB * NB * (int)sizeof(float);
+
+template <int NSLOT>
+__device__ __forceinline__ void chain_drain(uint64_t* full, int q0, int q1, int32_t* err) {
+  for (int q = q0; q < q1; ++q) mbar_wait_bounded(&full[q % NSLOT], (uint32_t)(q / NSLOT) & 1u, TS_WAIT_LIMIT);
+  atomicExch(err, 1);
+}
+
+// acc[q] += Σ_c box[c][rl + q] · v[c] over the columns c = g, g + G, … of a box (FP32
+// products of the vector's high and low parts summed in chunks of 16, folded into the
+// float-float accumulators)
+template <int G>
+__device__ __forceinline__ void box_rows(SweepAcc<float> (&acc)[4], const float* __restrict__ box, int rl, int g,
+                                         const float2* __restrict__ v) {
+  constexpr int CPG = NB / G, CU = CPG < 16 ? CPG : 16;
+#pragma unroll
+  for (int c0 = 0; c0 < CPG; c0 += CU) {
+    float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int u = 0; u < CU; ++u) {
+      const int c = g + G * (c0 + u);
+      const float4 m = *reinterpret_cast<const float4*>(box + c * NB + rl);
+      const float2 vv = v[c];
+      h[0] = fmaf(m.x, vv.x, h[0]); l[0] = fmaf(m.x, vv.y, l[0]);
+      h[1] = fmaf(m.y, vv.x, h[1]); l[1] = fmaf(m.y, vv.y, l[1]);
+      h[2] = fmaf(m.z, vv.x, h[2]); l[2] = fmaf(m.z, vv.y, l[2]);
+      h[3] = fmaf(m.w, vv.x, h[3]); l[3] = fmaf(m.w, vv.y, l[3]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[q].merge(h[q], l[q]);
+  }
+}
+
+template <int G>
+__device__ __forceinline__ void merge_groups(SweepAcc<float> (&acc)[4]) {
+  constexpr int LPR = 32 / G;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int o = LPR; o < 32; o <<= 1)
+      acc[q].merge(__shfl_xor_sync(0xffffffffu, acc[q].hi, o), __shfl_xor_sync(0xffffffffu, acc[q].lo, o));
+}
+
+// Forward chain (unit lower), the semantics of k_tri_fwd: for the NB-blocks k of [s0, s1) in
+// order, t[block j] −= M[block j, block k] t[block k] for the blocks j > k of the
+// super-block.  Boxes in step order: (k, j) for j = k+1 … nb−1.
+template <int G, int NSLOT>
+__global__ void __launch_bounds__(128 * G) k_chain_fwd(const __grid_constant__ CUtensorMap map, int64_t first,
+                                                       double* __restrict__ tsave, const int64_t* __restrict__ toff,
+                                                       const double* __restrict__ b, const int32_t* __restrict__ elim,
+                                                       const int64_t* __restrict__ elim_ptr,
+                                                       const int32_t* __restrict__ f_ne, int E, int s0, int s1,
+                                                       int gather, int32_t* err, long wait_limit) {
+  constexpr int LPR = 32 / G;
+  extern __shared__ __align__(1024) unsigned char ch_raw[];
+  float* slots = reinterpret_cast<float*>(ch_raw);  // [NSLOT][NB columns][NB rows]
+  __shared__ __align__(8) uint64_t full[NSLOT];
+  __shared__ float2 vb[NB];
+  __shared__ int abort_flag;
+  const int fl = blockIdx.x;
+  const int64_t f = first + fl;
+  double* t = tsave + toff[f];
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int lane = threadIdx.x & 31, g = lane / LPR;
+  const int rq = (threadIdx.x >> 5) * LPR + lane % LPR;  // row quad of the super-block
+  const int r0 = s0 + 4 * rq, jb = rq / (NB / 4), rl = 4 * (rq % (NB / 4));
+  const int nb = (s1 - s0 + NB - 1) / NB, nbox = nb * (nb - 1) / 2;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSLOT; ++s) mbar_init(&full[s], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int qi = 0, ik = 0, ij = 1;  // next box to issue and its (column block, row block): thread 0
+  auto issue = [&](int qend) {
+    for (; qi < qend; ++qi) {
+      const int s = qi % NSLOT;
+      mbar_expect_tx(&full[s], CH_BOX_BYTES);
+      tma_load_3d(slots + (size_t)s * NB * NB, &map, s0 + NB * ij, s0 + NB * ik, fl, &full[s]);
+      if (++ij == nb) { ++ik; ij = ik + 1; }
+    }
+  };
+  if (threadIdx.x == 0) issue(min(nbox, NSLOT));
+  if (gather)
+    for (int i = threadIdx.x; i < E; i += blockDim.x)
+      if (i < s0 || i >= s1) t[i] = i < ne ? b[el[i]] : 0.0;
+  ChainVal<float> tr[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int r = r0 + q;
+    tr[q].set(r < s1 ? (gather ? (r < ne ? b[el[r]] : 0.0) : t[r]) : 0.0);
+  }
+  int qc = 0;  // first box of the current step
+  for (int k = 0; k + 1 < nb; ++k) {
+    if (g == 0 && jb == k)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) vb[rl + q] = tr[q].packed();
+    __syncthreads();
+    SweepAcc<float> acc[4];
+    const bool active = jb > k && r0 < s1;
+    if (active) {
+      const int q = qc + (jb - k - 1);
+      if (mbar_wait_bounded(&full[q % NSLOT], (uint32_t)(q / NSLOT) & 1u, wait_limit))
+        box_rows<G>(acc, slots + (size_t)(q % NSLOT) * NB * NB, rl, g, vb);
+      else
+        abort_flag = 1;
+    }
+    if constexpr (G > 1) merge_groups<G>(acc);
+    if (active)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tr[q].sub(acc[q]);
+    __syncthreads();  // the step's boxes are consumed
+    const int qn = qc + (nb - 1 - k);
+    if (abort_flag) {
+      if (threadIdx.x == 0) chain_drain<NSLOT>(full, qc, qi, err);
+      return;
+    }
+    qc = qn;
+    if (threadIdx.x == 0) issue(min(nbox, qc + NSLOT));
+  }
+  if (g == 0)
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (r0 + q < s1) t[r0 + q] = tr[q].value();
+}
+
+// Backward chain (block upper with the stored block inverses), right-looking, the semantics
+// of k_tri_bwd: for the NB-blocks k of [s0, s1) in reverse, x_k = D_k⁻¹ z_k, then
+// z[block j] −= M[block j, block k] x_k for the blocks j < k.  Writes x[elim[i]] for i < ne.
+// Boxes in step order: (k, k) (the inverse), then (j, k) for j = 0 … k−1.
+template <int G, int NSLOT>
+__global__ void __launch_bounds__(128 * G) k_chain_bwd(const __grid_constant__ CUtensorMap map, int64_t first,
+                                                       const double* __restrict__ tsave,
+                                                       const int64_t* __restrict__ toff, double* __restrict__ x,
+                                                       const int32_t* __restrict__ elim,
+                                                       const int64_t* __restrict__ elim_ptr,
+                                                       const int32_t* __restrict__ f_ne, int s0, int s1,
+                                                       int32_t* err, long wait_limit) {
+  constexpr int LPR = 32 / G;
+  extern __shared__ __align__(1024) unsigned char ch_raw[];
+  float* slots = reinterpret_cast<float*>(ch_raw);
+  __shared__ __align__(8) uint64_t full[NSLOT];
+  __shared__ float2 vb[NB], xb[NB];
+  __shared__ int abort_flag;
+  const int fl = blockIdx.x;
+  const int64_t f = first + fl;
+  const double* z = tsave + toff[f];
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int lane = threadIdx.x & 31, g = lane / LPR;
+  const int rq = (threadIdx.x >> 5) * LPR + lane % LPR;
+  const int r0 = s0 + 4 * rq, jb = rq / (NB / 4), rl = 4 * (rq % (NB / 4));
+  const int nb = (s1 - s0 + NB - 1) / NB, nbox = nb * (nb + 1) / 2;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSLOT; ++s) mbar_init(&full[s], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int qi = 0, ik = nb - 1, ij = -1;  // ij = −1: the inverse block of step ik
+  auto issue = [&](int qend) {
+    for (; qi < qend; ++qi) {
+      const int s = qi % NSLOT;
+      const int row = ij < 0 ? ik : ij;
+      mbar_expect_tx(&full[s], CH_BOX_BYTES);
+      tma_load_3d(slots + (size_t)s * NB * NB, &map, s0 + NB * row, s0 + NB * ik, fl, &full[s]);
+      if (++ij == ik) { --ik; ij = -1; }
+    }
+  };
+  if (threadIdx.x == 0) issue(min(nbox, NSLOT));
+  ChainVal<float> tr[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) tr[q].set(r0 + q < s1 ? z[r0 + q] : 0.0);
+  int qc = 0;
+  for (int k = nb - 1; k >= 0; --k) {
+    const float2 zero2 = make_float2(0.f, 0.f);
+    if (g == 0 && jb == k)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) vb[rl + q] = r0 + q < s1 ? tr[q].packed() : zero2;
+    __syncthreads();
+    // x_k = D_k⁻¹ z_k (the threads of row block k)
+    SweepAcc<float> acc[4];
+    if (jb == k) {
+      if (mbar_wait_bounded(&full[qc % NSLOT], (uint32_t)(qc / NSLOT) & 1u, wait_limit))
+        box_rows<G>(acc, slots + (size_t)(qc % NSLOT) * NB * NB, rl, g, vb);
+      else
+        abort_flag = 1;
+    }
+    if constexpr (G > 1) merge_groups<G>(acc);
+    if (jb == k && g == 0)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = r0 + q;
+        xb[rl + q] = r < s1 ? acc_packed(acc[q]) : zero2;
+        if (r < ne) x[el[r]] = acc[q].value();
+      }
+    __syncthreads();
+    // z_j −= M[block j, block k] x_k (the threads of the row blocks j < k)
+    SweepAcc<float> a2[4];
+    if (jb < k) {
+      const int q = qc + 1 + jb;
+      if (mbar_wait_bounded(&full[q % NSLOT], (uint32_t)(q / NSLOT) & 1u, wait_limit))
+        box_rows<G>(a2, slots + (size_t)(q % NSLOT) * NB * NB, rl, g, xb);
+      else
+        abort_flag = 1;
+    }
+    if constexpr (G > 1) merge_groups<G>(a2);
+    if (jb < k)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tr[q].sub(a2[q]);
+    __syncthreads();
+    if (abort_flag) {
+      if (threadIdx.x == 0) chain_drain<NSLOT>(full, qc, qi, err);
+      return;
+    }
+    qc += k + 1;
+    if (threadIdx.x == 0) issue(min(nbox, qc + NSLOT));
+  }
+}
+
 // ------------------------------------------------------------------ host drivers
 // ---- tensor maps of the TMA-staged sweeps
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -1605,12 +1838,24 @@ static void build_sweep_maps(MFNumeric* M) {
   M->maps.assign(2 * nl, CUtensorMap{});
   M->map_rows.assign(2 * nl, 0);
   M->map_ok.assign(nl, 0);
+  M->cmaps.assign(nl, CUtensorMap{});
+  M->cmap_ok.assign(nl, 0);
   M->maps_base = M->F;
   EncodeTiledFn enc = encode_tiled_fn();
   if (!enc) return;
   float* F = reinterpret_cast<float*>(M->F);
   for (size_t l = 0; l < nl; ++l) {
     const MFLevel& L = S.levels[l];
+    // chain boxes: NB rows x NB columns of one front (16-byte row coordinates: NB-aligned)
+    if (L.n >= NB && L.n % 4 == 0 && L.off % 4 == 0 && L.count <= (1LL << 31) - 1) {
+      const cuuint64_t dims[3] = {(cuuint64_t)L.n, (cuuint64_t)L.n, (cuuint64_t)L.count};
+      const cuuint64_t strides[2] = {(cuuint64_t)L.n * sizeof(float), (cuuint64_t)L.n * L.n * sizeof(float)};
+      const cuuint32_t box[3] = {NB, NB, 1};
+      const cuuint32_t estr[3] = {1, 1, 1};
+      M->cmap_ok[l] = enc(&M->cmaps[l], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, F + L.off, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
     if (L.n < TS_ROWS || L.count > (1 << 16)) continue;
     bool ok = true;
     for (int dir = 0; dir < 2; ++dir) {  // 0: forward (B rows), 1: backward (E rows)
@@ -1891,6 +2136,44 @@ static int gemv_t_cols(const gbmhd_ctx* ctx, int cols, int cnt) {
   return 1;
 }
 
+// TMA-staged chain of one super-block [s0, s1) of level l (FP32 factors with a chain map).
+// Levels with many fronts: 128-thread CTAs and a ring of just enough slots for one step
+// (several CTAs per SM); levels with few fronts: 512 threads and 12 slots (one CTA per SM,
+// the ring a step and a half ahead).
+template <int G, int NS>
+static int chain_launch(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0, int s1, int gather,
+                        const double* b, double* x) {
+  const MFLevel& L = M->S.levels[l];
+  const DevSym& d = M->d;
+  const int sm = NS * CH_BOX_BYTES;
+  if (fwd) {
+    MF_CUDA(cudaFuncSetAttribute(k_chain_fwd<G, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    k_chain_fwd<G, NS><<<(unsigned)L.count, 128 * G, sm, ctx->stream>>>(
+        M->cmaps[l], L.first, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.E, s0, s1, gather,
+        M->d_sweep_err, M->wait_limit);
+  } else {
+    MF_CUDA(cudaFuncSetAttribute(k_chain_bwd<G, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    k_chain_bwd<G, NS><<<(unsigned)L.count, 128 * G, sm, ctx->stream>>>(
+        M->cmaps[l], L.first, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, s0, s1,
+        M->d_sweep_err, M->wait_limit);
+  }
+  gbmhd::count_launch();
+  MF_CUDA(cudaGetLastError());
+  return 0;
+}
+
+static_assert(SB / NB <= 8, "the ring variants below hold the blocks of one step (nb <= 8)");
+static int chain_tma(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0, int s1, int gather, const double* b,
+                     double* x) {
+  const int nb = (s1 - s0 + NB - 1) / NB;
+  if (M->S.levels[l].count >= 2 * ctx->num_sms) {
+    if (nb <= 4) return chain_launch<1, 4>(ctx, M, l, fwd, s0, s1, gather, b, x);
+    if (nb <= 6) return chain_launch<1, 6>(ctx, M, l, fwd, s0, s1, gather, b, x);
+    return chain_launch<1, 8>(ctx, M, l, fwd, s0, s1, gather, b, x);
+  }
+  return chain_launch<4, 12>(ctx, M, l, fwd, s0, s1, gather, b, x);
+}
+
 // One application of the factors: x = A⁻¹ b (or A⁻ᵀ b when tr) on the factorized dofs.  Per
 // level (forward bottom-up, backward top-down) and per super-block: the substitution chain
 // (k_tri_*), then the GEMV beyond the super-block (k_rect / k_rect_tma, or k_rect_t for the
@@ -1954,7 +2237,9 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       const int gather = s0 == 0;  // the first chain reads t = b[elim] for the whole front
       if (!tr) {
         constexpr int R = RowVec<T>::R;
-        if (sizeof(T) == 8 || wide)
+        if (sizeof(T) == 4 && M->cmap_ok[l]) {
+          if ((rc = chain_tma(ctx, M, l, true, s0, s1, gather, b, x))) return rc;
+        } else if (sizeof(T) == 8 || wide)
           { k_tri_fwd<T, 1><<<cnt, SB / R, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
         else
           { k_tri_fwd<T, TRI_G(4)><<<cnt, SB / R * TRI_G(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
@@ -1975,7 +2260,9 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       if (!tr) {
         if ((rc = rect((size_t)l, 1, s0, s1, s1, n, 1))) return rc;
         constexpr int W1 = 32 * NB / RowVec<T>::R / 4;  // threads of one column-group set
-        if (cnt >= ctx->num_sms || sizeof(T) == 8)
+        if (sizeof(T) == 4 && M->cmap_ok[l]) {
+          if ((rc = chain_tma(ctx, M, l, false, s0, s1, 0, b, x))) return rc;
+        } else if (cnt >= ctx->num_sms || sizeof(T) == 8)
           { k_tri_bwd<T, 1><<<cnt, W1, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
         else
           { k_tri_bwd<T, TRI_GH(4)><<<cnt, W1 * TRI_GH(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
