@@ -311,8 +311,9 @@ def run_ours(args):
     pk = peaks()
     asm_achieved = alg_bytes / (jac_ms / 1e3) / 1e9
     # dominant kernels: the multifrontal solve sweeps; algorithmic bytes = the FP32 factor
-    # entries one preconditioner application reads (forward: nb x ne per front, backward:
-    # ne x (ne + nb)), timed by CUDA events on the context stream around every application
+    # entries one preconditioner application reads (forward: the unit-lower L, E²/2 + nb·E
+    # per front; backward: U with the block inverses, E²/2 + E·nb), timed by CUDA events on
+    # the context stream around every application
     sw_achieved = sw_bytes * sw_n / sw_s / 1e9 if sw_s > 0 else None
     extra = {} if args.no_compare else compare_paths(args, ctx, mesh, dm, d_x, stream, opts)
     line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
@@ -333,8 +334,9 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "cells/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
             "gpu_launches": int(L1["launches"] - L0["launches"]),
             "library_gemm_calls": int(L1["gemm_calls"] - L0["gemm_calls"]),
-            "roofline": {"kernel": "multifrontal solve sweeps (k_sweep_tma<1> forward + k_sweep_tma<0> backward over all levels, one preconditioner "
-                                   "application)", "bound": "hbm",
+            "roofline": {"kernel": "multifrontal preconditioner application: one CUDA graph launch of the LU sweeps "
+                                   "(k_chain_fwd + k_rect_tma forward, k_rect_tma + k_chain_bwd backward, over all "
+                                   "levels and super-blocks)", "bound": "hbm",
                          "achieved": sw_achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
                          "frac": sw_achieved / pk.get("hbm_gbs") if sw_achieved else None,
                          "traffic": None, "bytes_per_application": sw_bytes, "applications": sw_n,

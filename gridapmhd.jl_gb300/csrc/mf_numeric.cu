@@ -48,6 +48,8 @@ struct MFNumeric {
   size_t F_bytes = 0;
   void* Pbuf = nullptr;        // diagonal-block inverses  [count][NB*NB]
   void* Cbuf = nullptr;        // column block below a pivot block [count][n*NB]
+  void* gws = nullptr;         // split images of the FP32 GEMM operands (tc_gemm.cu)
+  size_t gws_bytes = 0;
   size_t work_bytes = 0;
   double* tsave = nullptr;     // per front: E slots holding t, y and z of a solve
   int64_t* tsave_off = nullptr;  // per front
@@ -209,6 +211,7 @@ void mf_destroy(MFNumeric* M) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (M->blas) cublasDestroy(M->blas);
+  if (M->gws) cudaFree(M->gws);
   if (M->vpk) cudaFree(M->vpk);
   if (M->d_dr) cudaFree(M->d_dr);
   if (M->d_dc) cudaFree(M->d_dc);
@@ -1801,6 +1804,192 @@ __global__ void __launch_bounds__(128 * G) k_chain_bwd(const __grid_constant__ C
   }
 }
 
+// Transposed chains (the adjoint's solves) on the same boxes.  A column of a box is 64
+// contiguous floats in shared memory: eight lanes per column (rows 4j + 32u, u = 0, 1: 16-byte
+// loads, conflict-free), partial sums of 8 products per lane folded into float-float and
+// reduced over the eight lanes with shuffles; 512 threads take the 64 columns of a box per
+// pass.  The super-block's vector segment lives in shared memory (float-float).
+constexpr int CT_THREADS = 512;
+
+// Σ_r box[c][r] v[r] over this lane's 8 rows, added to acc
+__device__ __forceinline__ void box_col8(SweepAcc<float>& acc, const float* __restrict__ box, int c, int j,
+                                         const float2* __restrict__ v) {
+  float h = 0.0f, l = 0.0f;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int r = 4 * j + 32 * u;
+    const float4 m = *reinterpret_cast<const float4*>(box + c * NB + r);
+    const float2 v0 = v[r], v1 = v[r + 1], v2 = v[r + 2], v3 = v[r + 3];
+    h = fmaf(m.x, v0.x, h); l = fmaf(m.x, v0.y, l);
+    h = fmaf(m.y, v1.x, h); l = fmaf(m.y, v1.y, l);
+    h = fmaf(m.z, v2.x, h); l = fmaf(m.z, v2.y, l);
+    h = fmaf(m.w, v3.x, h); l = fmaf(m.w, v3.y, l);
+  }
+  acc.merge(h, l);
+}
+
+// Transposed forward chain (Uᵀ: block lower with D⁻ᵀ), the semantics of k_tri_fwd_t: for the
+// NB-blocks k of [s0, s1) in order, y_k = D_k⁻ᵀ t_k, then t[block j] −= M[block k, block j]ᵀ y_k
+// for j > k.  Boxes in step order: (k, k), then (k, j) for j = k+1 … nb−1.
+template <int NSLOT>
+__global__ void __launch_bounds__(CT_THREADS) k_chain_fwd_t(const __grid_constant__ CUtensorMap map, int64_t first,
+                                                            double* __restrict__ tsave,
+                                                            const int64_t* __restrict__ toff,
+                                                            const double* __restrict__ b,
+                                                            const int32_t* __restrict__ elim,
+                                                            const int64_t* __restrict__ elim_ptr,
+                                                            const int32_t* __restrict__ f_ne, int E, int s0, int s1,
+                                                            int gather, int32_t* err, long wait_limit) {
+  extern __shared__ __align__(1024) unsigned char ch_raw[];
+  float* slots = reinterpret_cast<float*>(ch_raw);
+  __shared__ __align__(8) uint64_t full[NSLOT];
+  __shared__ float2 tt[SB], yb[NB];
+  __shared__ int abort_flag;
+  const int fl = blockIdx.x;
+  const int64_t f = first + fl;
+  double* t = tsave + toff[f];
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int j = threadIdx.x % 8, cs = threadIdx.x / 8;  // lane in the column, column of a box
+  const int len = s1 - s0, nb = (len + NB - 1) / NB, nbox = nb * (nb + 1) / 2;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSLOT; ++s) mbar_init(&full[s], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int qi = 0, ik = 0, ij = -1;  // ij = −1: the inverse block of step ik
+  auto issue = [&](int qend) {
+    for (; qi < qend; ++qi) {
+      const int s = qi % NSLOT;
+      mbar_expect_tx(&full[s], CH_BOX_BYTES);
+      tma_load_3d(slots + (size_t)s * NB * NB, &map, s0 + NB * ik, s0 + NB * (ij < 0 ? ik : ij), fl, &full[s]);
+      ij = ij < 0 ? ik + 1 : ij + 1;
+      if (ij == nb) { ++ik; ij = -1; }
+    }
+  };
+  if (threadIdx.x == 0) issue(min(nbox, NSLOT));
+  for (int i = threadIdx.x; i < SB; i += blockDim.x) tt[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+  if (gather) {
+    for (int i = threadIdx.x; i < E; i += blockDim.x) {
+      const double v = i < ne ? b[el[i]] : 0.0;
+      if (i >= s0 && i < s1) tt[i - s0] = SweepAcc<float>::pack(v);
+      else t[i] = v;
+    }
+  } else {
+    for (int i = threadIdx.x; i < len; i += blockDim.x) tt[i] = SweepAcc<float>::pack(t[s0 + i]);
+  }
+  __syncthreads();
+  int qc = 0;
+  for (int k = 0; k < nb; ++k) {
+    const int kb = min(NB, len - NB * k);
+    // (a) y_c = Σ_r D⁻¹[r, c] t_r
+    SweepAcc<float> acc;
+    if (mbar_wait_bounded(&full[qc % NSLOT], (uint32_t)(qc / NSLOT) & 1u, wait_limit))
+      box_col8(acc, slots + (size_t)(qc % NSLOT) * NB * NB, cs, j, tt + NB * k);
+    else
+      abort_flag = 1;
+    acc.warp_reduce8();
+    __syncthreads();  // every lane has read t of block k
+    if (j == 0 && cs < kb) {
+      tt[NB * k + cs] = acc_packed(acc);
+      yb[cs] = acc_packed(acc);
+    }
+    if (j == 0 && cs >= kb) yb[cs] = make_float2(0.f, 0.f);
+    __syncthreads();
+    // (b) t[block jj] −= M[block k, block jj]ᵀ y_k
+    for (int jj = k + 1; jj < nb; ++jj) {
+      const int q = qc + (jj - k);
+      SweepAcc<float> a2;
+      if (mbar_wait_bounded(&full[q % NSLOT], (uint32_t)(q / NSLOT) & 1u, wait_limit))
+        box_col8(a2, slots + (size_t)(q % NSLOT) * NB * NB, cs, j, yb);
+      else
+        abort_flag = 1;
+      a2.warp_reduce8();
+      const int c = NB * jj + cs;
+      if (j == 0 && c < len) tt[c] = vsub(tt[c], a2);
+    }
+    __syncthreads();  // the step's boxes are consumed
+    if (abort_flag) {
+      if (threadIdx.x == 0) chain_drain<NSLOT>(full, qc, qi, err);
+      return;
+    }
+    qc += nb - k;
+    if (threadIdx.x == 0) issue(min(nbox, qc + NSLOT));
+  }
+  for (int i = threadIdx.x; i < len; i += blockDim.x) t[s0 + i] = vto(tt[i]);
+}
+
+// Transposed backward chain (Lᵀ: unit upper), the semantics of k_tri_bwd_t: for the NB-blocks k
+// of [s0, s1) in reverse, x_k = z_k − Σ_{j>k} M[block j, block k]ᵀ x_j; writes x[elim[i]] for
+// i < ne.  Boxes in step order: (j, k) for j = k+1 … nb−1.
+template <int NSLOT>
+__global__ void __launch_bounds__(CT_THREADS) k_chain_bwd_t(const __grid_constant__ CUtensorMap map, int64_t first,
+                                                            const double* __restrict__ tsave,
+                                                            const int64_t* __restrict__ toff, double* __restrict__ x,
+                                                            const int32_t* __restrict__ elim,
+                                                            const int64_t* __restrict__ elim_ptr,
+                                                            const int32_t* __restrict__ f_ne, int s0, int s1,
+                                                            int32_t* err, long wait_limit) {
+  extern __shared__ __align__(1024) unsigned char ch_raw[];
+  float* slots = reinterpret_cast<float*>(ch_raw);
+  __shared__ __align__(8) uint64_t full[NSLOT];
+  __shared__ float2 xv[SB];
+  __shared__ int abort_flag;
+  const int fl = blockIdx.x;
+  const int64_t f = first + fl;
+  const double* z = tsave + toff[f];
+  const int ne = f_ne[f];
+  const int32_t* el = elim + elim_ptr[f];
+  const int j = threadIdx.x % 8, cs = threadIdx.x / 8;
+  const int len = s1 - s0, nb = (len + NB - 1) / NB, nbox = nb * (nb - 1) / 2;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSLOT; ++s) mbar_init(&full[s], 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int qi = 0, ik = nb - 2, ij = nb - 1;  // step ik reads the boxes (ij, ik), ij = ik+1 … nb−1
+  auto issue = [&](int qend) {
+    for (; qi < qend; ++qi) {
+      const int s = qi % NSLOT;
+      mbar_expect_tx(&full[s], CH_BOX_BYTES);
+      tma_load_3d(slots + (size_t)s * NB * NB, &map, s0 + NB * ij, s0 + NB * ik, fl, &full[s]);
+      if (++ij == nb) { --ik; ij = ik + 1; }
+    }
+  };
+  if (threadIdx.x == 0) issue(min(nbox, NSLOT));
+  for (int i = threadIdx.x; i < SB; i += blockDim.x) xv[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+  int qc = 0;
+  for (int k = nb - 1; k >= 0; --k) {
+    const int kb = min(NB, len - NB * k);
+    SweepAcc<float> acc;
+    for (int jj = k + 1; jj < nb; ++jj) {
+      const int q = qc + (jj - k - 1);
+      if (mbar_wait_bounded(&full[q % NSLOT], (uint32_t)(q / NSLOT) & 1u, wait_limit))
+        box_col8(acc, slots + (size_t)(q % NSLOT) * NB * NB, cs, j, xv + NB * jj);
+      else
+        abort_flag = 1;
+    }
+    acc.warp_reduce8();
+    if (j == 0 && cs < kb) {
+      const int r = s0 + NB * k + cs;
+      const float2 v = vsub(SweepAcc<float>::pack(z[r]), acc);
+      xv[NB * k + cs] = v;
+      if (r < ne) x[el[r]] = vto(v);
+    }
+    __syncthreads();  // x of block k is visible, the step's boxes are consumed
+    if (abort_flag) {
+      if (threadIdx.x == 0) chain_drain<NSLOT>(full, qc, qi, err);
+      return;
+    }
+    qc += nb - 1 - k;
+    if (threadIdx.x == 0) issue(min(nbox, qc + NSLOT));
+  }
+}
+
 // ------------------------------------------------------------------ host drivers
 // ---- tensor maps of the TMA-staged sweeps
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -1896,7 +2085,7 @@ static int gemm(gbmhd_ctx* ctx, MFNumeric* M, int m, int n, int k, T alpha, cons
   if constexpr (sizeof(T) == 4) {
     std::string msg;
     const int rc = gbmhd::tc_gemm_f32(ctx->stream, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch,
-                                      M->d_err, &msg);
+                                      M->gws, M->gws_bytes, M->d_err, &msg);
     if (rc) ctx->err = "multifrontal: " + msg;
     return rc;
   } else {
@@ -1931,6 +2120,24 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
     MF_CUDA(cudaMalloc(&M->Pbuf, sizeof(T) * std::max<size_t>(pbytes, 1)));
     MF_CUDA(cudaMalloc(&M->Cbuf, sizeof(T) * std::max<size_t>(wmax, 1)));
     M->work_bytes = need;
+  }
+  if constexpr (sizeof(T) == 4) {
+    // the largest split workspace of the level's GEMMs: the first panel's L products
+    // (rb x kb x kb), U rows (kb x rest x ≤ PW) and trailing update (rest x rest x pw)
+    size_t gws = 0;
+    for (const MFLevel& L : S.levels) {
+      const int pw = std::min(PW, L.E), kb = std::min(NB, L.E), cnt = (int)L.count;
+      gws = std::max(gws, gbmhd::tc_gemm_workspace(L.n - kb, kb, kb, cnt));
+      gws = std::max(gws, gbmhd::tc_gemm_workspace(kb, L.n - pw, pw, cnt));
+      gws = std::max(gws, gbmhd::tc_gemm_workspace(L.n - pw, L.n - pw, pw, cnt));
+    }
+    if (M->gws_bytes < gws) {
+      if (M->gws) cudaFree(M->gws);
+      M->gws = nullptr;
+      M->gws_bytes = 0;
+      MF_CUDA(cudaMalloc(&M->gws, gws));
+      M->gws_bytes = gws;
+    }
   }
   T* F = reinterpret_cast<T*>(M->F);
   T* P = reinterpret_cast<T*>(M->Pbuf);
@@ -2162,7 +2369,40 @@ static int chain_launch(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0
   return 0;
 }
 
+template <int NS>
+static int chain_launch_t(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0, int s1, int gather,
+                          const double* b, double* x) {
+  const MFLevel& L = M->S.levels[l];
+  const DevSym& d = M->d;
+  const int sm = NS * CH_BOX_BYTES;
+  if (fwd) {
+    MF_CUDA(cudaFuncSetAttribute(k_chain_fwd_t<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    k_chain_fwd_t<NS><<<(unsigned)L.count, CT_THREADS, sm, ctx->stream>>>(
+        M->cmaps[l], L.first, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.E, s0, s1, gather,
+        M->d_sweep_err, M->wait_limit);
+  } else {
+    MF_CUDA(cudaFuncSetAttribute(k_chain_bwd_t<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    k_chain_bwd_t<NS><<<(unsigned)L.count, CT_THREADS, sm, ctx->stream>>>(
+        M->cmaps[l], L.first, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, s0, s1, M->d_sweep_err,
+        M->wait_limit);
+  }
+  gbmhd::count_launch();
+  MF_CUDA(cudaGetLastError());
+  return 0;
+}
+
 static_assert(SB / NB <= 8, "the ring variants below hold the blocks of one step (nb <= 8)");
+static int chain_tma_t(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0, int s1, int gather,
+                       const double* b, double* x) {
+  const int nb = (s1 - s0 + NB - 1) / NB;
+  if (M->S.levels[l].count >= 2 * ctx->num_sms) {
+    if (nb <= 4) return chain_launch_t<4>(ctx, M, l, fwd, s0, s1, gather, b, x);
+    if (nb <= 6) return chain_launch_t<6>(ctx, M, l, fwd, s0, s1, gather, b, x);
+    return chain_launch_t<8>(ctx, M, l, fwd, s0, s1, gather, b, x);
+  }
+  return chain_launch_t<12>(ctx, M, l, fwd, s0, s1, gather, b, x);
+}
+
 static int chain_tma(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0, int s1, int gather, const double* b,
                      double* x) {
   const int nb = (s1 - s0 + NB - 1) / NB;
@@ -2245,6 +2485,9 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
           { k_tri_fwd<T, TRI_G(4)><<<cnt, SB / R * TRI_G(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
         if ((rc = rect(l, 0, s1, n, s0, s1, 0))) return rc;
       } else {
+        if (sizeof(T) == 4 && M->cmap_ok[l]) {
+          if ((rc = chain_tma_t(ctx, M, l, true, s0, s1, gather, b, x))) return rc;
+        } else
         { k_tri_fwd_t<T><<<cnt, TT_THREADS, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
         if ((rc = rect_t(l, s0, s1, s1, n, 0))) return rc;
       }
@@ -2268,6 +2511,9 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
           { k_tri_bwd<T, TRI_GH(4)><<<cnt, W1 * TRI_GH(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
       } else {
         if ((rc = rect_t((size_t)l, s1, n, s0, s1, 1))) return rc;
+        if (sizeof(T) == 4 && M->cmap_ok[l]) {
+          if ((rc = chain_tma_t(ctx, M, l, false, s0, s1, 0, b, x))) return rc;
+        } else
         { k_tri_bwd_t<T><<<cnt, TT_THREADS, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr,
               d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
       }

@@ -1,7 +1,7 @@
 """ctypes binding of libgbmhd (include/gbmhd.h).
 
 This is the reference-facing boundary as a Python host sees it; the Julia
-host binds the same symbols with ``ccall``.  There is no
+host binds the same symbols with ``ccall`` (julia/GridapMHDGB300.jl).  There is no
 CPU fallback: if the CUDA library is missing or no GPU is present, calls fail.
 """
 from __future__ import annotations

@@ -9,12 +9,13 @@
 * 48x48x4 duct (β = 2.5, Ha = 200, Re = 10, cw = 0.1, f_z ~ U[0.9, 1.1] per cell, seed 0):
   the adjoint gradient of the axial flow rate at mid-length w.r.t. Ha, cw and the f_z field
   (along a direction of positive per-cell weights, seed 1), against central finite differences
-  of FP64 GPU Newton solves (step 1e-6 relative), and
+  of FP64 GPU Newton solves (relative steps 1e-6 and 1e-4), and
   against the gradient formed with the oracle's FP64 assembly (its residual at the GPU state,
   its transposed Jacobian applied to the GPU's λ, and its ∂R/∂θ).
 
 Tolerances: 1e-8 relative L2 per field (pressure modulo a constant); 1e-6 relative on every
-gradient component.
+gradient component against the oracle-assembly gradient and the 1e-4-step differences, 1e-5
+against the 1e-6-step differences (their noise floor, see the test).
 """
 import os
 
@@ -79,10 +80,11 @@ def test_cfg4_48x48x4_adjoint_gradient(gpu_lib):
     g = flow_rate(mesh, dm, 0.1)
     ctx = gpu_context(mesh, dm, params)
     base = dict(precision=0, restart=200, max_linear=600)
-    # to the FP64 residual's floor (the assembly round-off, ~1e-12 absolute at γ = 4000)
+    # to the FP64 residual's floor: the round-off of the assembly, whose atomic adds run in
+    # arbitrary order, at γ = 4000 (measured 1e-12 … 5e-11 absolute from run to run)
     x, rep, rc = ctx.newton_solve(np.zeros(dm.ndofs), max_newton=12, newton_rtol=1e-14, newton_atol=0.0,
                                   linear_rtol=1e-12, **base)
-    assert rep["final_residual"] <= 1e-9 * rep["initial_residual"], rep
+    assert rep["final_residual"] <= 2e-8 * rep["initial_residual"], rep
     dJ, lam, arep, arc = ctx.adjoint(x, g, with_cells=True, linear_rtol=1e-10, **base)
     assert arc == 0, arep
     dJ_dHa = ha_gradient(dJ, Ha, Re, "cfd")
@@ -91,7 +93,7 @@ def test_cfg4_48x48x4_adjoint_gradient(gpu_lib):
     prob = oracle_problem(mesh, dm, params)
     r0, _ = prob.residual_jacobian(np.zeros(dm.ndofs), want_jac=False)
     r, A = prob.residual_jacobian(x)
-    assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(r0), (np.linalg.norm(r), np.linalg.norm(r0))
+    assert np.linalg.norm(r) <= 2e-8 * np.linalg.norm(r0), (np.linalg.norm(r), np.linalg.norm(r0))
     assert np.linalg.norm(A.T @ lam - g) <= 1e-9 * np.linalg.norm(g)
     dRg, dRc, fzm = oracle_param_derivs(prob, x)
     gd = dm.global_cell_dofs()[:, 54:81]
@@ -102,8 +104,11 @@ def test_cfg4_48x48x4_adjoint_gradient(gpu_lib):
     dfz_ref = np.sum(lz * fzm, 1)
     assert np.linalg.norm(dJ[4:] - dfz_ref) <= 1e-6 * np.linalg.norm(dfz_ref)
 
-    # (2) central finite differences of FP64 GPU Newton solves from x, step 1e-6 relative
-    h = 1e-6
+    # (2) central finite differences of FP64 GPU Newton solves from x.  The J of a solve carries
+    # the FP64 residual floor (1e-12 … 5e-11 absolute, the assembly's atomic adds in arbitrary
+    # order): measured 3e-14 … 1.4e-13 in J, i.e. up to ~5e-6 of the gradient at a relative
+    # step of 1e-6.  So the 1e-6 step is checked to 1e-5, and a 1e-4 step (truncation
+    # O(h²) ~ 1e-8, noise 100x smaller) to the 1e-6 target.
     fd_opts = dict(max_newton=6, newton_rtol=0.0, newton_atol=0.0, linear_rtol=1e-12, **base)
 
     def J(p):
@@ -111,23 +116,22 @@ def test_cfg4_48x48x4_adjoint_gradient(gpu_lib):
         xs, _, _ = ctx.newton_solve(x, **fd_opts)
         return g @ xs
 
-    fd = {}
-    pp = dict(params, gamma=(Ha * (1 + h)) ** 2 / Re)
-    pm = dict(params, gamma=(Ha * (1 - h)) ** 2 / Re)
-    fd["Ha"] = (J(pp) - J(pm)) / (2 * h * Ha)
     f = params["facets"]
-    fd["cw"] = (J(dict(params, facets=dict(f, cw=f["cw"] * (1 + h)))) -
-                J(dict(params, facets=dict(f, cw=f["cw"] * (1 - h))))) / (2 * h * f["cw"][0])
-    # a direction of positive weights: the flow rate responds to it at the size of J itself, so
-    # the difference of two solves stays well above their convergence floor (a zero-mean random
-    # direction gives dJ·w ~ 1e-5 J, where that floor is ~1e-4 of the difference)
     w = np.random.default_rng(1).uniform(0.5, 1.5, mesh.ncells) * params["f_cell"][:, 2]
-    fp, fm = params["f_cell"].copy(), params["f_cell"].copy()
-    fp[:, 2] += h * w
-    fm[:, 2] -= h * w
-    fd["f_z"] = (J(dict(params, f_cell=fp)) - J(dict(params, f_cell=fm))) / (2 * h)
-    ctx.set_params(params)
     adj = {"Ha": dJ_dHa, "cw": dJ[1], "f_z": float(dJ[4:] @ w)}
-    print("cfg4 gradient: adjoint", adj, "finite differences", fd)
-    for k in adj:
-        assert abs(fd[k] - adj[k]) <= 1e-6 * abs(adj[k]), (k, fd[k], adj[k])
+    for h, tol in ((1e-6, 1e-5), (1e-4, 1e-6)):
+        fd = {}
+        pp = dict(params, gamma=(Ha * (1 + h)) ** 2 / Re)
+        pm = dict(params, gamma=(Ha * (1 - h)) ** 2 / Re)
+        fd["Ha"] = (J(pp) - J(pm)) / (2 * h * Ha)
+        fd["cw"] = (J(dict(params, facets=dict(f, cw=f["cw"] * (1 + h)))) -
+                    J(dict(params, facets=dict(f, cw=f["cw"] * (1 - h))))) / (2 * h * f["cw"][0])
+        fp, fm = params["f_cell"].copy(), params["f_cell"].copy()
+        fp[:, 2] += h * w
+        fm[:, 2] -= h * w
+        fd["f_z"] = (J(dict(params, f_cell=fp)) - J(dict(params, f_cell=fm))) / (2 * h)
+        ctx.set_params(params)
+        print(f"cfg4 gradient, step {h:g}: adjoint", adj, "finite differences", fd,
+              "relative", {k: abs(fd[k] - adj[k]) / abs(adj[k]) for k in adj})
+        for k in adj:
+            assert abs(fd[k] - adj[k]) <= tol * abs(adj[k]), (h, k, fd[k], adj[k])

@@ -39,17 +39,18 @@ def _load(d, name, dt):
 def symbolic(harness, mesh, dm, mono):
     gd = np.ascontiguousarray(dm.global_cell_dofs().astype(np.int32))
     X = np.ascontiguousarray(mesh.cell_coords())
-    d = tempfile.mkdtemp()
-    rc = harness.mf_harness(C.c_int64(mesh.ncells), X.ctypes.data_as(C.c_void_p), gd.ctypes.data_as(C.c_void_p),
-                            C.c_int64(dm.ndofs), C.c_int(1 if mono else 0), d.encode())
-    assert rc == 0
-    S = {k: _load(d, k, t) for k, t in (("rowptr", np.int64), ("col", np.int32), ("levels", np.int64),
-                                        ("f_ne", np.int32), ("f_nb", np.int32), ("f_level", np.int32),
-                                        ("f_parent", np.int32), ("f_off", np.int64), ("elim_ptr", np.int64),
-                                        ("bnd_ptr", np.int64), ("elim", np.int32), ("bnd", np.int32),
-                                        ("ah_src", np.int32), ("ah_dst", np.int64), ("child_list", np.int32),
-                                        ("ea_ptr", np.int64), ("ea_pos", np.int32), ("reg_dst", np.int64),
-                                        ("reg_dof", np.int32), ("sizes", np.int64))}
+    with tempfile.TemporaryDirectory() as d:  # the arrays are read into memory, the files removed
+        rc = harness.mf_harness(C.c_int64(mesh.ncells), X.ctypes.data_as(C.c_void_p),
+                                gd.ctypes.data_as(C.c_void_p), C.c_int64(dm.ndofs), C.c_int(1 if mono else 0),
+                                d.encode())
+        assert rc == 0
+        S = {k: _load(d, k, t) for k, t in (("rowptr", np.int64), ("col", np.int32), ("levels", np.int64),
+                                            ("f_ne", np.int32), ("f_nb", np.int32), ("f_level", np.int32),
+                                            ("f_parent", np.int32), ("f_off", np.int64), ("elim_ptr", np.int64),
+                                            ("bnd_ptr", np.int64), ("elim", np.int32), ("bnd", np.int32),
+                                            ("ah_src", np.int32), ("ah_dst", np.int64), ("child_list", np.int32),
+                                            ("ea_ptr", np.int64), ("ea_pos", np.int32), ("reg_dst", np.int64),
+                                            ("reg_dof", np.int32), ("sizes", np.int64))}
     S["levels"] = S["levels"].reshape(-1, 10)
     return S
 
