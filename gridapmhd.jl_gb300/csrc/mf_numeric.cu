@@ -4,6 +4,7 @@
 
 #include <cstdlib>
 #include <cstring>
+#include <utility>
 
 #include "mf.h"
 #include "tc_gemm.h"
@@ -1481,6 +1482,15 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// Programmatic dependent launch: the sweep kernels are launched so that they may start while
+// the kernel before them finishes.  Everything before pdl_wait() (barrier set-up and the TMA
+// copies of factor blocks, which no kernel of a solve writes) overlaps that kernel's tail;
+// pdl_wait() returns once the previous kernel has completed and its writes are visible, and
+// only then are the solve's vectors read or written.  pdl_trigger() after it lets the next
+// kernel start its own set-up.  Launched without the attribute, both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // out[r] −= Σ_{c ∈ [c0, c1)} M[r, c] v[c] for r ∈ [r0, r1) (the semantics of k_rect) with the
 // front's columns streamed through shared memory by TMA.  CTA (row tile, column chunk,
 // front): thread 0 issues the stage copies; every wait is bounded (wait_limit spins), and a
@@ -1525,6 +1535,8 @@ __global__ void __launch_bounds__(TS_THREADS) k_rect_tma(const __grid_constant__
   double* t = tsave + toff[f];
   const int32_t* el = elim + elim_ptr[f];
   const int32_t* bd = bnd + bnd_ptr[f];
+  pdl_wait();
+  pdl_trigger();
   for (int c = threadIdx.x; c < ncol; c += blockDim.x)
     vs[c] = SweepAcc<float>::pack(front_vec(ca + c, E, ne, nb, t, x, el, bd, from_x));
   __syncthreads();
@@ -1667,6 +1679,8 @@ __global__ void __launch_bounds__(128 * G) k_chain_fwd(const __grid_constant__ C
     }
   };
   if (threadIdx.x == 0) issue(min(nbox, NSLOT));
+  pdl_wait();
+  pdl_trigger();
   if (gather)
     for (int i = threadIdx.x; i < E; i += blockDim.x)
       if (i < s0 || i >= s1) t[i] = i < ne ? b[el[i]] : 0.0;
@@ -1754,6 +1768,8 @@ __global__ void __launch_bounds__(128 * G) k_chain_bwd(const __grid_constant__ C
     }
   };
   if (threadIdx.x == 0) issue(min(nbox, NSLOT));
+  pdl_wait();
+  pdl_trigger();
   ChainVal<float> tr[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) tr[q].set(r0 + q < s1 ? z[r0 + q] : 0.0);
@@ -1871,6 +1887,8 @@ __global__ void __launch_bounds__(CT_THREADS) k_chain_fwd_t(const __grid_constan
   if (threadIdx.x == 0) issue(min(nbox, NSLOT));
   for (int i = threadIdx.x; i < SB; i += blockDim.x) tt[i] = make_float2(0.f, 0.f);
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
   if (gather) {
     for (int i = threadIdx.x; i < E; i += blockDim.x) {
       const double v = i < ne ? b[el[i]] : 0.0;
@@ -1962,6 +1980,8 @@ __global__ void __launch_bounds__(CT_THREADS) k_chain_bwd_t(const __grid_constan
   if (threadIdx.x == 0) issue(min(nbox, NSLOT));
   for (int i = threadIdx.x; i < SB; i += blockDim.x) xv[i] = make_float2(0.f, 0.f);
   __syncthreads();
+  pdl_wait();
+  pdl_trigger();
   int qc = 0;
   for (int k = nb - 1; k >= 0; --k) {
     const int kb = min(NB, len - NB * k);
@@ -2343,6 +2363,25 @@ static int gemv_t_cols(const gbmhd_ctx* ctx, int cols, int cnt) {
   return 1;
 }
 
+// Launch with programmatic stream serialization (the kernel's pdl_wait() orders it after the
+// previous kernel of the stream; see pdl_wait).  Captured into the application's graph as a
+// programmatic edge.
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 // TMA-staged chain of one super-block [s0, s1) of level l (FP32 factors with a chain map).
 // Levels with many fronts: 128-thread CTAs and a ring of just enough slots for one step
 // (several CTAs per SM); levels with few fronts: 512 threads and 12 slots (one CTA per SM,
@@ -2355,14 +2394,18 @@ static int chain_launch(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0
   const int sm = NS * CH_BOX_BYTES;
   if (fwd) {
     MF_CUDA(cudaFuncSetAttribute(k_chain_fwd<G, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    k_chain_fwd<G, NS><<<(unsigned)L.count, 128 * G, sm, ctx->stream>>>(
-        M->cmaps[l], L.first, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.E, s0, s1, gather,
-        M->d_sweep_err, M->wait_limit);
+    MF_CUDA(cudaFuncSetAttribute(k_chain_fwd<G, NS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    MF_CUDA(launch_pdl(k_chain_fwd<G, NS>, dim3((unsigned)L.count), dim3(128 * G), sm, ctx->stream, M->cmaps[l],
+                       L.first, M->tsave, (const int64_t*)M->tsave_off, b, (const int32_t*)d.elim,
+                       (const int64_t*)d.elim_ptr, (const int32_t*)d.f_ne, L.E, s0, s1, gather, M->d_sweep_err,
+                       M->wait_limit));
   } else {
     MF_CUDA(cudaFuncSetAttribute(k_chain_bwd<G, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    k_chain_bwd<G, NS><<<(unsigned)L.count, 128 * G, sm, ctx->stream>>>(
-        M->cmaps[l], L.first, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, s0, s1,
-        M->d_sweep_err, M->wait_limit);
+    MF_CUDA(cudaFuncSetAttribute(k_chain_bwd<G, NS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    MF_CUDA(launch_pdl(k_chain_bwd<G, NS>, dim3((unsigned)L.count), dim3(128 * G), sm, ctx->stream, M->cmaps[l],
+                       L.first, (const double*)M->tsave, (const int64_t*)M->tsave_off, x, (const int32_t*)d.elim,
+                       (const int64_t*)d.elim_ptr, (const int32_t*)d.f_ne, s0, s1, M->d_sweep_err,
+                       M->wait_limit));
   }
   gbmhd::count_launch();
   MF_CUDA(cudaGetLastError());
@@ -2377,14 +2420,18 @@ static int chain_launch_t(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int 
   const int sm = NS * CH_BOX_BYTES;
   if (fwd) {
     MF_CUDA(cudaFuncSetAttribute(k_chain_fwd_t<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    k_chain_fwd_t<NS><<<(unsigned)L.count, CT_THREADS, sm, ctx->stream>>>(
-        M->cmaps[l], L.first, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.E, s0, s1, gather,
-        M->d_sweep_err, M->wait_limit);
+    MF_CUDA(cudaFuncSetAttribute(k_chain_fwd_t<NS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    MF_CUDA(launch_pdl(k_chain_fwd_t<NS>, dim3((unsigned)L.count), dim3(CT_THREADS), sm, ctx->stream, M->cmaps[l],
+                       L.first, M->tsave, (const int64_t*)M->tsave_off, b, (const int32_t*)d.elim,
+                       (const int64_t*)d.elim_ptr, (const int32_t*)d.f_ne, L.E, s0, s1, gather, M->d_sweep_err,
+                       M->wait_limit));
   } else {
     MF_CUDA(cudaFuncSetAttribute(k_chain_bwd_t<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-    k_chain_bwd_t<NS><<<(unsigned)L.count, CT_THREADS, sm, ctx->stream>>>(
-        M->cmaps[l], L.first, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, s0, s1, M->d_sweep_err,
-        M->wait_limit);
+    MF_CUDA(cudaFuncSetAttribute(k_chain_bwd_t<NS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    MF_CUDA(launch_pdl(k_chain_bwd_t<NS>, dim3((unsigned)L.count), dim3(CT_THREADS), sm, ctx->stream, M->cmaps[l],
+                       L.first, (const double*)M->tsave, (const int64_t*)M->tsave_off, x, (const int32_t*)d.elim,
+                       (const int64_t*)d.elim_ptr, (const int32_t*)d.f_ne, s0, s1, M->d_sweep_err,
+                       M->wait_limit));
   }
   gbmhd::count_launch();
   MF_CUDA(cudaGetLastError());
@@ -2436,9 +2483,13 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       dim3 g((unsigned)((r1 - r0 + rows - 1) / rows), (unsigned)((c1 - c0 + cw - 1) / cw), (unsigned)cnt);
       const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
       MF_CUDA(cudaFuncSetAttribute(k_rect_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      { k_rect_tma<<<g, rows / 2, sm, ctx->stream>>>(M->maps[2 * l + dir], L.first, L.E, r0, r1, c0, c1, rows, cw,
-            M->tsave, M->tsave_off, x, b, d.elim, d.elim_ptr, d.bnd, d.bnd_ptr, d.f_ne, d.f_nb, from_x,
-            M->d_sweep_err, M->wait_limit); gbmhd::count_launch(); }
+      MF_CUDA(cudaFuncSetAttribute(k_rect_tma, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+      MF_CUDA(launch_pdl(k_rect_tma, g, dim3(rows / 2), sm, ctx->stream, M->maps[2 * l + dir], L.first, L.E, r0, r1, c0,
+                         c1, rows, cw, M->tsave, (const int64_t*)M->tsave_off, (const double*)x, b,
+                         (const int32_t*)d.elim, (const int64_t*)d.elim_ptr, (const int32_t*)d.bnd,
+                         (const int64_t*)d.bnd_ptr, (const int32_t*)d.f_ne, (const int32_t*)d.f_nb, from_x,
+                         M->d_sweep_err, M->wait_limit));
+      gbmhd::count_launch();
     } else {
       const int cols = sweep_cols(ctx, r1 - r0, c1 - c0, cnt, rows_cta);
       dim3 g((unsigned)((r1 - r0 + rows_cta - 1) / rows_cta), (unsigned)((c1 - c0 + cols - 1) / cols), (unsigned)cnt);
