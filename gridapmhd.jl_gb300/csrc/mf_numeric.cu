@@ -253,21 +253,39 @@ __global__ void k_arrowhead(const V* __restrict__ Aval, const int32_t* __restric
 // scales its right-hand side by Dr and its result by Dc.  Measured at Ha = 500 on the 64x64x4
 // duct (FP32 emulation): the worst 64x64 pivot blocks drop from κ ~1e12 to ~1e9 and the FGMRES
 // iterations per three digits from 20 to 11.
+// The maxima run in the value precision: the scale factors are powers of two, so |a_ij|·r_i·c_j
+// is exact in FP32 for the FP32 Jacobian (and only its power of two matters), and the 32-bit
+// bit patterns of non-negative floats order like the floats.  GB300 issues FP64 at a small
+// fraction of its FP32 rate: the FP64 version of this pass was FP64-issue bound.
+template <typename V>
+struct RuizBits;
+template <>
+struct RuizBits<float> {
+  using U = unsigned int;
+  __device__ static U bits(float a) { return __float_as_uint(a); }
+  __device__ static float value(U u) { return __uint_as_float(u); }
+};
+template <>
+struct RuizBits<double> {
+  using U = unsigned long long;
+  __device__ static U bits(double a) { return (unsigned long long)__double_as_longlong(a); }
+  __device__ static double value(U u) { return __longlong_as_double((long long)u); }
+};
+
 template <typename V>
 __global__ void k_ruiz_max(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                           const V* __restrict__ val, const double* __restrict__ dr, const double* __restrict__ dc,
-                           double* __restrict__ rmax, unsigned long long* __restrict__ cmax) {
+                           const V* __restrict__ val, const V* __restrict__ dr, const V* __restrict__ dc,
+                           V* __restrict__ rmax, typename RuizBits<V>::U* __restrict__ cmax) {
   const int lane = threadIdx.x & 31;
   for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < n;
        r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const double sr = dr[r];
-    double m = 0.0;
+    const V sr = dr[r];
+    V m = 0;
     for (int64_t t = rowptr[r] + lane; t < rowptr[r + 1]; t += 32) {
       const int32_t c = col[t];
-      const double a = fabs((double)val[t] * sr * dc[c]);
+      const V a = fabs(val[t] * sr * dc[c]);
       m = fmax(m, a);
-      // non-negative doubles order like their bit patterns
-      atomicMax(&cmax[c], (unsigned long long)__double_as_longlong(a));
+      atomicMax(&cmax[c], RuizBits<V>::bits(a));
     }
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
     if (lane == 0) rmax[r] = m;
@@ -279,24 +297,34 @@ __device__ __forceinline__ double pow2_rsqrt(double m) {  // 2^round(-log2(m)/2)
   return exp2(rint(-0.5 * log2(m)));
 }
 
-__global__ void k_ruiz_update(int64_t n, const double* __restrict__ rmax, const unsigned long long* __restrict__ cmax,
-                              double* __restrict__ dr, double* __restrict__ dc) {
+// dr, dc (FP64) and their copies in the value precision (drv, dcv) take the new factors
+template <typename V>
+__global__ void k_ruiz_update(int64_t n, const V* __restrict__ rmax, const typename RuizBits<V>::U* __restrict__ cmax,
+                              double* __restrict__ dr, double* __restrict__ dc, V* __restrict__ drv,
+                              V* __restrict__ dcv) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    dr[i] *= pow2_rsqrt(rmax[i]);
-    dc[i] *= pow2_rsqrt(__longlong_as_double((long long)cmax[i]));
+    dr[i] *= pow2_rsqrt((double)rmax[i]);
+    dc[i] *= pow2_rsqrt((double)RuizBits<V>::value(cmax[i]));
+    drv[i] = (V)dr[i];
+    dcv[i] = (V)dc[i];
   }
 }
 
 template <typename V>
 __global__ void k_scale_vals(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-                             const V* __restrict__ val, const double* __restrict__ dr, const double* __restrict__ dc,
+                             const V* __restrict__ val, const V* __restrict__ dr, const V* __restrict__ dc,
                              V* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < n;
        r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const V sr = (V)dr[r];  // powers of two: exact in V
-    for (int64_t t = rowptr[r] + lane; t < rowptr[r + 1]; t += 32) out[t] = val[t] * sr * (V)dc[col[t]];
+    const V sr = dr[r];  // powers of two: exact in V
+    for (int64_t t = rowptr[r] + lane; t < rowptr[r + 1]; t += 32) out[t] = val[t] * sr * dc[col[t]];
   }
+}
+
+template <typename T>
+__global__ void k_fill_t(int64_t n, T a, T* __restrict__ v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) v[i] = a;
 }
 
 __global__ void k_fill(int64_t n, double a, double* __restrict__ v) {
@@ -1652,7 +1680,7 @@ __global__ void __launch_bounds__(128 * G) k_chain_fwd(const __grid_constant__ C
   extern __shared__ __align__(1024) unsigned char ch_raw[];
   float* slots = reinterpret_cast<float*>(ch_raw);  // [NSLOT][NB columns][NB rows]
   __shared__ __align__(8) uint64_t full[NSLOT];
-  __shared__ float2 vb[NB];
+  __shared__ float2 vb[2][NB];
   __shared__ int abort_flag;
   const int fl = blockIdx.x;
   const int64_t f = first + fl;
@@ -1690,18 +1718,25 @@ __global__ void __launch_bounds__(128 * G) k_chain_fwd(const __grid_constant__ C
     const int r = r0 + q;
     tr[q].set(r < s1 ? (gather ? (r < ne ? b[el[r]] : 0.0) : t[r]) : 0.0);
   }
-  int qc = 0;  // first box of the current step
-  for (int k = 0; k + 1 < nb; ++k) {
-    if (g == 0 && jb == k)
+  // One barrier per step: at its top t_k is in vb[k & 1] (published by the threads of block k
+  // at the end of the step before) and the boxes of the step before are consumed.
+  if (g == 0 && jb == 0)
 #pragma unroll
-      for (int q = 0; q < 4; ++q) vb[rl + q] = tr[q].packed();
+    for (int q = 0; q < 4; ++q) vb[0][rl + q] = tr[q].packed();
+  int qc = 0, qprev = 0;  // first box of the current and of the previous step
+  for (int k = 0; k + 1 < nb; ++k) {
     __syncthreads();
+    if (abort_flag) {
+      if (threadIdx.x == 0) chain_drain<NSLOT>(full, qprev, qi, err);
+      return;
+    }
+    if (threadIdx.x == 0 && k > 0) issue(min(nbox, qc + NSLOT));
     SweepAcc<float> acc[4];
     const bool active = jb > k && r0 < s1;
     if (active) {
       const int q = qc + (jb - k - 1);
       if (mbar_wait_bounded(&full[q % NSLOT], (uint32_t)(q / NSLOT) & 1u, wait_limit))
-        box_rows<G>(acc, slots + (size_t)(q % NSLOT) * NB * NB, rl, g, vb);
+        box_rows<G>(acc, slots + (size_t)(q % NSLOT) * NB * NB, rl, g, vb[k & 1]);
       else
         abort_flag = 1;
     }
@@ -1709,14 +1744,16 @@ __global__ void __launch_bounds__(128 * G) k_chain_fwd(const __grid_constant__ C
     if (active)
 #pragma unroll
       for (int q = 0; q < 4; ++q) tr[q].sub(acc[q]);
-    __syncthreads();  // the step's boxes are consumed
-    const int qn = qc + (nb - 1 - k);
-    if (abort_flag) {
-      if (threadIdx.x == 0) chain_drain<NSLOT>(full, qc, qi, err);
-      return;
-    }
-    qc = qn;
-    if (threadIdx.x == 0) issue(min(nbox, qc + NSLOT));
+    qprev = qc;
+    qc += nb - 1 - k;
+    if (g == 0 && jb == k + 1)  // block k + 1 is final: publish it for the next step
+#pragma unroll
+      for (int q = 0; q < 4; ++q) vb[(k + 1) & 1][rl + q] = tr[q].packed();
+  }
+  __syncthreads();  // the last step's boxes are consumed
+  if (abort_flag) {
+    if (threadIdx.x == 0) chain_drain<NSLOT>(full, qprev, qi, err);
+    return;
   }
   if (g == 0)
 #pragma unroll
@@ -1773,13 +1810,21 @@ __global__ void __launch_bounds__(128 * G) k_chain_bwd(const __grid_constant__ C
   ChainVal<float> tr[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) tr[q].set(r0 + q < s1 ? z[r0 + q] : 0.0);
-  int qc = 0;
-  for (int k = nb - 1; k >= 0; --k) {
-    const float2 zero2 = make_float2(0.f, 0.f);
-    if (g == 0 && jb == k)
+  // Two barriers per step: at the top of step k, z_k is in vb (published by the threads of block
+  // k at the end of the step before) and the boxes of the step before are consumed; the second
+  // publishes x_k.
+  const float2 zero2 = make_float2(0.f, 0.f);
+  if (g == 0 && jb == nb - 1)
 #pragma unroll
-      for (int q = 0; q < 4; ++q) vb[rl + q] = r0 + q < s1 ? tr[q].packed() : zero2;
+    for (int q = 0; q < 4; ++q) vb[rl + q] = r0 + q < s1 ? tr[q].packed() : zero2;
+  int qc = 0, qprev = 0;
+  for (int k = nb - 1; k >= 0; --k) {
     __syncthreads();
+    if (abort_flag) {
+      if (threadIdx.x == 0) chain_drain<NSLOT>(full, qprev, qi, err);
+      return;
+    }
+    if (threadIdx.x == 0 && k < nb - 1) issue(min(nbox, qc + NSLOT));
     // x_k = D_k⁻¹ z_k (the threads of row block k)
     SweepAcc<float> acc[4];
     if (jb == k) {
@@ -1810,14 +1855,14 @@ __global__ void __launch_bounds__(128 * G) k_chain_bwd(const __grid_constant__ C
     if (jb < k)
 #pragma unroll
       for (int q = 0; q < 4; ++q) tr[q].sub(a2[q]);
-    __syncthreads();
-    if (abort_flag) {
-      if (threadIdx.x == 0) chain_drain<NSLOT>(full, qc, qi, err);
-      return;
-    }
+    qprev = qc;
     qc += k + 1;
-    if (threadIdx.x == 0) issue(min(nbox, qc + NSLOT));
+    if (g == 0 && jb == k - 1)  // block k − 1 is final: publish it for the next step
+#pragma unroll
+      for (int q = 0; q < 4; ++q) vb[rl + q] = r0 + q < s1 ? tr[q].packed() : zero2;
   }
+  __syncthreads();  // the last step's boxes are consumed
+  if (abort_flag && threadIdx.x == 0) chain_drain<NSLOT>(full, qprev, qi, err);
 }
 
 // Transposed chains (the adjoint's solves) on the same boxes.  A column of a box is 64
@@ -2289,23 +2334,31 @@ static int equilibrate(gbmhd_ctx* ctx, MFNumeric* M, const V* val) {
     MF_CUDA(cudaMalloc(&M->d_sval, sizeof(V) * std::max<int64_t>(nnz, 1)));
     M->sval_bytes = sizeof(V) * (size_t)nnz;
   }
-  double* rmax = nullptr;
-  unsigned long long* cmax = nullptr;
-  MF_CUDA(cudaMallocAsync(&rmax, sizeof(double) * std::max<int64_t>(n, 1), ctx->stream));
-  MF_CUDA(cudaMallocAsync(&cmax, sizeof(unsigned long long) * std::max<int64_t>(n, 1), ctx->stream));
+  using U = typename RuizBits<V>::U;
+  V* rmax = nullptr;
+  U* cmax = nullptr;
+  V *drv = nullptr, *dcv = nullptr;  // the factors in the value precision
+  MF_CUDA(cudaMallocAsync(&rmax, sizeof(V) * std::max<int64_t>(n, 1), ctx->stream));
+  MF_CUDA(cudaMallocAsync(&cmax, sizeof(U) * std::max<int64_t>(n, 1), ctx->stream));
+  MF_CUDA(cudaMallocAsync(&drv, sizeof(V) * std::max<int64_t>(n, 1), ctx->stream));
+  MF_CUDA(cudaMallocAsync(&dcv, sizeof(V) * std::max<int64_t>(n, 1), ctx->stream));
   const unsigned gw = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, (int64_t)ctx->num_sms * 16));
   const unsigned gv = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)ctx->num_sms * 8));
   { k_fill<<<gv, 256, 0, ctx->stream>>>(n, 1.0, M->d_dr); gbmhd::count_launch(); }
   { k_fill<<<gv, 256, 0, ctx->stream>>>(n, 1.0, M->d_dc); gbmhd::count_launch(); }
+  { k_fill_t<V><<<gv, 256, 0, ctx->stream>>>(n, (V)1, drv); gbmhd::count_launch(); }
+  { k_fill_t<V><<<gv, 256, 0, ctx->stream>>>(n, (V)1, dcv); gbmhd::count_launch(); }
   for (int it = 0; it < 3; ++it) {
-    MF_CUDA(cudaMemsetAsync(cmax, 0, sizeof(unsigned long long) * n, ctx->stream));
-    { k_ruiz_max<V><<<gw, 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, val, M->d_dr, M->d_dc, rmax, cmax); gbmhd::count_launch(); }
-    { k_ruiz_update<<<gv, 256, 0, ctx->stream>>>(n, rmax, cmax, M->d_dr, M->d_dc); gbmhd::count_launch(); }
+    MF_CUDA(cudaMemsetAsync(cmax, 0, sizeof(U) * n, ctx->stream));
+    { k_ruiz_max<V><<<gw, 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, val, drv, dcv, rmax, cmax); gbmhd::count_launch(); }
+    { k_ruiz_update<V><<<gv, 256, 0, ctx->stream>>>(n, rmax, cmax, M->d_dr, M->d_dc, drv, dcv); gbmhd::count_launch(); }
   }
-  { k_scale_vals<V><<<gw, 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, val, M->d_dr, M->d_dc, reinterpret_cast<V*>(M->d_sval)); gbmhd::count_launch(); }
+  { k_scale_vals<V><<<gw, 256, 0, ctx->stream>>>(n, ctx->d_rowptr, ctx->d_col, val, drv, dcv, reinterpret_cast<V*>(M->d_sval)); gbmhd::count_launch(); }
   MF_CUDA(cudaGetLastError());
   MF_CUDA(cudaFreeAsync(rmax, ctx->stream));
   MF_CUDA(cudaFreeAsync(cmax, ctx->stream));
+  MF_CUDA(cudaFreeAsync(drv, ctx->stream));
+  MF_CUDA(cudaFreeAsync(dcv, ctx->stream));
   return 0;
 }
 

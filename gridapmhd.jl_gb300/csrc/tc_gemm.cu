@@ -24,13 +24,14 @@
 //         (M = 128, N = 128, K = 16) per stage into the tile's FP32 accumulator (128
 //         tensor-memory columns), commits each stage to its `empty` barrier and each tile
 //         to `acc_full`;
-//       warps 2-5 (epilogue): the C tile is copied into shared memory with cp.async before
-//         the accumulator is ready; warp w then reads accumulator lanes 32·(w mod 4).. with
-//         tcgen05.ld in chunks of 32 columns, writes α·acc + β·C with coalesced column
-//         accesses and arrives on `acc_empty`.
+//       warps 2-5 (epilogue): C moves in chunks of 32 columns through a ring of four
+//         shared-memory buffers, loaded by TMA three chunks ahead and written back by TMA
+//         stores (one thread issues both); warp w combines accumulator lanes 32·(w mod 4)..
+//         (tcgen05.ld) with the chunk in place and arrives on `acc_empty` after each tile.
 // Every wait is bounded.  One that runs out sets *err = 2 and an abort flag that ends the
 // other roles' loops; the MMA thread then waits (bounded) for its MMAs in flight before the
 // tensor memory is freed, and the tiles not finished are left unwritten.
+#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's driver entry point)
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -46,7 +47,9 @@ constexpr int NST = 3;                      // stages in the ring
 constexpr int PART_BYTES = TM * KC * 2;     // one BF16 part of one 128-row block and stage: 8 KB
 constexpr int IMG_BYTES = 3 * PART_BYTES;   // the three parts of one operand stage: 24 KB
 constexpr int STAGE_BYTES = 2 * IMG_BYTES;  // A parts 0..2, B parts 0..2
-constexpr int CTILE_BYTES = TM * TN * 4;    // the C tile staged for the epilogue: 64 KB
+constexpr int CW = 32, NCB = 4;            // C chunks of 32 columns, a ring of 4 buffers
+constexpr int CHUNK_BYTES = CW * TM * 4;    // 16 KB
+constexpr int CTILE_BYTES = NCB * CHUNK_BYTES;  // the C ring of the epilogue: 64 KB
 constexpr int PROD_WARP = 0, MMA_WARP = 1, EPI_WARP0 = 2, EPI_WARPS = 4;
 constexpr int TC_THREADS = 32 * (EPI_WARP0 + EPI_WARPS);
 constexpr int ACC_COLS = 2 * TN;            // two accumulators
@@ -93,13 +96,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
-__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -150,6 +146,18 @@ __device__ __forceinline__ TileCoord tile_coord(int64_t tile, int mt, int nt) {
   return c;
 }
 
+__device__ __forceinline__ void tma_load_c(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_c(const CUtensorMap* map, int x, int y, int z, const void* src) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
+               ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(src))
+               : "memory");
+}
+
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
@@ -197,11 +205,12 @@ __global__ void __launch_bounds__(TM) k_tc_split(int m, int n, int k, const floa
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_tc_gemm(int m, int n, int k, float alpha, const unsigned char* __restrict__ ws, float beta,
-              float* __restrict__ C, int ldc, long long sC, int batch, int c16, int32_t* err) {
+    k_tc_gemm(const __grid_constant__ CUtensorMap cmap, int tma_c, int m, int n, int k, float alpha,
+              const unsigned char* __restrict__ ws, float beta, float* __restrict__ C, int ldc, long long sC,
+              int batch, int c16, int32_t* err) {
   // [NST][A parts 0..2 | B parts 0..2], then the C tile [TN columns][TM rows]
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  __shared__ __align__(8) uint64_t full[NST], empty[NST], acc_full[2], acc_empty[2], drain_bar;
+  __shared__ __align__(8) uint64_t full[NST], empty[NST], acc_full[2], acc_empty[2], drain_bar, cfull[NCB];
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   volatile int* abort_v = &abort_flag;
@@ -225,6 +234,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&acc_empty[b])), "r"(32 * EPI_WARPS));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&drain_bar)));
+    for (int i = 0; i < NCB; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&cfull[i])));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
   }
@@ -308,37 +318,42 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncwarp();
   } else {
     // ---------------------------------------------------------------- epilogue
-    // The C tile is copied into shared memory with cp.async before the accumulator is ready
-    // (4096 16-byte pieces, or single entries where C is not 16-byte aligned or rows run
-    // out), then row gi of the tile is written from tensor-memory lane gi.
-    const int q = warp & 3, et = tid - 32 * EPI_WARP0;  // lane quadrant; 0..127
+    // With a tensor map of C (tma_c): C moves in chunks of CW = 32 columns through a ring of
+    // NCB = 4 shared-memory buffers [CW columns][TM rows]; thread 0 of the epilogue loads a
+    // chunk with one TMA box copy three chunks ahead, the four warps combine it in place with
+    // the accumulator columns (tcgen05.ld, lane = row), and thread 0 writes it back with one
+    // TMA store (one bulk group per chunk; a buffer is reused once the store of its previous
+    // chunk has read it).  TMA clips the box at the edges of C.  Without a tensor map (C or
+    // its strides not 16-byte aligned) row gi is written directly from lane gi.
+    const int q = warp & 3, et = tid - 32 * EPI_WARP0;
+    const bool leader = et == 0;
     float* Cs = reinterpret_cast<float*>(tc_smem + (size_t)NST * STAGE_BYTES);
+    const int64_t my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t nchunks = my_tiles * NCB;
+    const bool loads = tma_c && beta != 0.0f;
+    auto issue_load = [&](int64_t g) {  // leader only
+      const TileCoord tc = tile_coord(blockIdx.x + (g / NCB) * gridDim.x, mt, nt);
+      const int bb = (int)(g % NCB);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&cfull[bb])),
+                   "r"((uint32_t)CHUNK_BYTES)
+                   : "memory");
+      tma_load_c(Cs + (size_t)bb * CW * TM, &cmap, tc.mi * TM, tc.nj * TN + bb * CW, (int)tc.bz, &cfull[bb]);
+    };
+    // every chunk is loaded, in order: the load of chunk g is the (g / NCB)-th into its buffer
+    int64_t issued = 0;  // chunks whose load has been issued (leader)
+    int64_t drain_from = -1;  // the first chunk whose wait ran out (leader)
+    if (leader && loads)
+      for (; issued < (nchunks < NCB - 1 ? nchunks : (int64_t)(NCB - 1)); ++issued) issue_load(issued);
     int b = 0;
     uint32_t aph = 0;
+    int64_t gc = 0;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
       const TileCoord tc = tile_coord(tile, mt, nt);
       const int i0 = tc.mi * TM, j0 = tc.nj * TN;
       float* Cb = C + tc.bz * sC;
-      if (beta != 0.0f) {
-        for (int e = et; e < (TM / 4) * TN; e += 32 * EPI_WARPS) {
-          const int col = e / (TM / 4), r4 = 4 * (e % (TM / 4));
-          const int gi = i0 + r4, gj = j0 + col;
-          if (gj >= n || gi >= m) continue;
-          float* dst = Cs + col * TM + r4;
-          const float* src = Cb + gi + (int64_t)gj * ldc;
-          if (c16 && gi + 3 < m) {
-            cp_async16(dst, src);
-          } else {
-            for (int u = 0; u < 4 && gi + u < m; ++u) cp_async4(dst + u, src + u);
-          }
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-      }
       const bool ok = mbar_wait(&acc_full[b], aph, abort_v);
-      asm volatile("cp.async.wait_all;" ::: "memory");
-      // the C tile is complete; the stop decision is reduced over the epilogue warps so that
-      // all of them leave together (the tensor-memory loads below are .sync.aligned, and
-      // the named barrier counts all four warps)
+      // the stop decision is reduced over the epilogue warps so that all of them leave together
+      // (the tensor-memory loads below are .sync.aligned, and the named barriers count all four)
       uint32_t stop;
       asm volatile(
           "{\n .reg .pred pin, pout;\n setp.ne.u32 pin, %1, 0;\n bar.red.or.pred pout, 1, %2, pin;\n"
@@ -349,8 +364,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (stop) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
       const int rl = 32 * q + lane, gi = i0 + rl;
-#pragma unroll 1
-      for (int c0 = 0; c0 < TN; c0 += 32) {
+      for (int c = 0; c < NCB; ++c, ++gc) {
+        const int c0 = CW * c;
         uint32_t r[32];
         const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * TN + c0);
         asm volatile(
@@ -362,20 +377,55 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (gi < m)
+        if (tma_c) {
+          const int bb = (int)(gc % NCB);
+          float* buf = Cs + (size_t)bb * CW * TM;
+          if (loads) {
+            if (!mbar_wait(&cfull[bb], (uint32_t)(gc / NCB) & 1u, abort_v)) {
+              *abort_v = 1;
+              if (leader && drain_from < 0) drain_from = gc;
+            }
+          } else {  // buf is free once the store of its previous chunk has read it
+            if (leader) asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(NCB - 1) : "memory");
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");
+          }
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const int gj = j0 + c0 + c;
-            if (gj < n) {
-              const float cv = beta != 0.0f ? beta * Cs[(c0 + c) * TM + rl] : 0.0f;
-              Cb[gi + (int64_t)gj * ldc] = fmaf(alpha, __uint_as_float(r[c]), cv);
+          for (int cc = 0; cc < 32; ++cc) {
+            float* e = buf + cc * TM + rl;
+            *e = fmaf(alpha, __uint_as_float(r[cc]), loads ? beta * *e : 0.0f);
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");  // the chunk is complete
+          if (leader) {
+            tma_store_c(&cmap, i0, j0 + c0, (int)tc.bz, buf);
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            if (loads && issued < nchunks) {
+              // the next load goes into the buffer whose store was committed one chunk ago
+              asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+              issue_load(issued++);
             }
           }
+        } else if (gi < m) {
+#pragma unroll
+          for (int cc = 0; cc < 32; ++cc) {
+            const int gj = j0 + c0 + cc;
+            if (gj < n) {
+              float* e = Cb + gi + (int64_t)gj * ldc;
+              *e = fmaf(alpha, __uint_as_float(r[cc]), beta != 0.0f ? beta * *e : 0.0f);
+            }
+          }
+        }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
       mbar_arrive(&acc_empty[b]);  // the accumulator may be overwritten
-      asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");  // the C tile may be overwritten
       if (++b == 2) { b = 0; aph ^= 1u; }
+    }
+    if (leader && tma_c) {
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");  // the stores have completed
+      // loads issued for chunks not consumed (an abort): let them land before the CTA leaves
+      for (int64_t g2 = drain_from >= 0 ? drain_from : gc; g2 < issued; ++g2)
+        for (long w = 0; w < TC_WAIT_LIMIT && !mbar_test(&cfull[g2 % NCB], (uint32_t)(g2 / NCB) & 1u); ++w) {
+        }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -387,6 +437,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }  // namespace
 
 constexpr size_t kTcSmem = (size_t)NST * STAGE_BYTES + CTILE_BYTES;  // 208 KB: one CTA per SM
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled_fn() {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q{};
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    return reinterpret_cast<EncodeTiledFn>(p);
+  return nullptr;
+}
 
 size_t tc_gemm_workspace(int m, int n, int k, int batch) {
   if (m <= 0 || n <= 0 || k <= 0 || batch <= 0) return 0;
@@ -432,8 +495,24 @@ int tc_gemm_f32(cudaStream_t stream, int m, int n, int k, float alpha, const flo
   const unsigned grid = (unsigned)std::min<int64_t>(tiles, std::max(1, num_sms));
   // 16-byte C pieces: the base, the column stride and the problem stride keep 16-byte alignment
   const int c16 = (reinterpret_cast<uintptr_t>(C) % 16 == 0 && ldc % 4 == 0 && sC % 4 == 0) ? 1 : 0;
-  k_tc_gemm<<<grid, TC_THREADS, kTcSmem, stream>>>(m, n, k, alpha, static_cast<const unsigned char*>(ws), beta, C,
-                                                   ldc, sC, batch, c16, err);
+  // the epilogue's tensor map of C: rows x columns x problems, box TM rows x CW columns
+  CUtensorMap cmap{};
+  int tma_c = 0;
+  if (c16 && (batch == 1 || sC > 0)) {
+    static EncodeTiledFn enc = encode_tiled_fn();
+    if (enc) {
+      const cuuint64_t dims[3] = {(cuuint64_t)m, (cuuint64_t)n, (cuuint64_t)batch};
+      const cuuint64_t strides[2] = {(cuuint64_t)ldc * sizeof(float),
+                                     (cuuint64_t)(batch > 1 ? sC : (long long)ldc * n) * sizeof(float)};
+      const cuuint32_t box[3] = {(cuuint32_t)TM, (cuuint32_t)CW, 1};
+      const cuuint32_t estr[3] = {1, 1, 1};
+      tma_c = enc(&cmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, C, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
+  }
+  k_tc_gemm<<<grid, TC_THREADS, kTcSmem, stream>>>(cmap, tma_c, m, n, k, alpha, static_cast<const unsigned char*>(ws),
+                                                   beta, C, ldc, sC, batch, c16, err);
   count_launch();
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
