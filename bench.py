@@ -35,7 +35,7 @@ CFG = dict(nc=(64, 64), nz=4, Lz=0.2, beta_map=3.0, Ha=500.0, Re=1.0, cw=0.1, ta
 SAMPLE_NC = (6, 6)      # bounded CPU sample per reference step
 SWEEP_NC = ((6, 6), (8, 8), (10, 10))
 # smaller duct for kernel-level profiling captures (fits a few GB on the device)
-CFG_SMALL = dict(nc=(32, 32), nz=3, Lz=0.2, beta_map=2.0, Ha=100.0, Re=10.0, cw=0.1, tau=100.0, zeta=0.0)
+CFG_SMALL = dict(nc=(32, 32), nz=4, Lz=0.2, beta_map=2.0, Ha=100.0, Re=10.0, cw=0.1, tau=100.0, zeta=0.0)
 METRIC = "Newton-solve throughput (cells/s), Hunt 64x64x4 Ha=500, mixed precision"
 
 
@@ -320,8 +320,10 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (Jacobian, preconditioner) / f64 (residual, Krylov, update)",
             "data": "synthetic",
-            "config": {"workload": "hunt duct 64x64x4, Lz=0.2, tanh(3x) stretching, Ha=500, Re=1, cw=0.1, "
-                                   f"zeta={ZETA}", "ncells": mesh.ncells, "ndofs": n, "nnz": ctx.nnz,
+            "config": {"workload": f"hunt duct {cfg['nc'][0]}x{cfg['nc'][1]}x{cfg['nz']}, Lz={cfg['Lz']}, "
+                                   f"tanh({cfg['beta_map']:g}x) stretching, Ha={cfg['Ha']:g}, Re={cfg['Re']:g}, "
+                                   f"cw={cfg['cw']:g}, zeta={cfg['zeta']:g}", "ncells": mesh.ncells, "ndofs": n,
+                       "nnz": ctx.nnz,
                        "precision": "mixed", "newton_rtol": 1e-12,
                        "l2": "inputs larger than L2 (Jacobian values alone 0.78 GB)"},
             "newton_solve_s": ms / 1e3, "newton_iters": last["newton_iters"], "linear_iters": last["linear_iters"],

@@ -82,6 +82,9 @@ struct MFNumeric {
   bool graphs_ok = true;            // capture failed once: launch directly
   // sweep timing: events around each solve, harvested when the next one starts
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // second stream of the sweeps: the GEMVs beyond the next super-block run beside the chains
+  cudaStream_t s2 = nullptr;
+  std::vector<cudaEvent_t> sev;      // a pool of events for the fork/join points of a solve
   bool ev_pending = false;
   int64_t sweep_applies = 0;
   double sweep_seconds = 0.0;
@@ -190,6 +193,9 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
   *M->h_sweep_err = 0;
   MF_CUDA(cudaEventCreate(&M->ev0));
   MF_CUDA(cudaEventCreate(&M->ev1));
+  MF_CUDA(cudaStreamCreateWithFlags(&M->s2, cudaStreamNonBlocking));
+  M->sev.assign(64, nullptr);
+  for (cudaEvent_t& e : M->sev) MF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   if ((rc = upload(ctx, &M->tsave_off, toff))) return rc;
   MF_CUDA(cudaMalloc(&M->tsave, sizeof(double) * std::max<int64_t>(t, 1)));
   MF_CUDA(cudaMalloc(&M->d_err, sizeof(int32_t)));
@@ -225,6 +231,9 @@ void mf_destroy(MFNumeric* M) {
   if (M->gx) cudaFree(M->gx);
   if (M->ev0) cudaEventDestroy(M->ev0);
   if (M->ev1) cudaEventDestroy(M->ev1);
+  for (cudaEvent_t e : M->sev)
+    if (e) cudaEventDestroy(e);
+  if (M->s2) cudaStreamDestroy(M->s2);
   delete M;
 }
 
@@ -2526,7 +2535,9 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
   const T* F = reinterpret_cast<const T*>(M->F);
   const DevSym& d = M->d;
   // out[r] −= M[r0:r1, c0:c1] v   (dir: 0 forward map, 1 backward map)
-  auto rect = [&](size_t l, int dir, int r0, int r1, int c0, int c1, int from_x) -> int {
+  auto rect = [&](size_t l, int dir, int r0, int r1, int c0, int c1, int from_x,
+                  cudaStream_t st = nullptr) -> int {
+    if (!st) st = ctx->stream;
     const MFLevel& L = S.levels[l];
     if (r1 <= r0 || c1 <= c0) return 0;
     const int cnt = (int)L.count;
@@ -2537,7 +2548,7 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       const size_t sm = (size_t)TS_STAGES * TS_COLS * rows * sizeof(float) + sizeof(float2) * cw;
       MF_CUDA(cudaFuncSetAttribute(k_rect_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       MF_CUDA(cudaFuncSetAttribute(k_rect_tma, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-      MF_CUDA(launch_pdl(k_rect_tma, g, dim3(rows / 2), sm, ctx->stream, M->maps[2 * l + dir], L.first, L.E, r0, r1, c0,
+      MF_CUDA(launch_pdl(k_rect_tma, g, dim3(rows / 2), sm, st, M->maps[2 * l + dir], L.first, L.E, r0, r1, c0,
                          c1, rows, cw, M->tsave, (const int64_t*)M->tsave_off, (const double*)x, b,
                          (const int32_t*)d.elim, (const int64_t*)d.elim_ptr, (const int32_t*)d.bnd,
                          (const int64_t*)d.bnd_ptr, (const int32_t*)d.f_ne, (const int32_t*)d.f_nb, from_x,
@@ -2546,7 +2557,7 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     } else {
       const int cols = sweep_cols(ctx, r1 - r0, c1 - c0, cnt, rows_cta);
       dim3 g((unsigned)((r1 - r0 + rows_cta - 1) / rows_cta), (unsigned)((c1 - c0 + cols - 1) / cols), (unsigned)cnt);
-      { k_rect<T><<<g, SW_THREADS, sizeof(V) * cols, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, b, d.elim,
+      { k_rect<T><<<g, SW_THREADS, sizeof(V) * cols, st>>>(F, d.f_off, M->tsave, M->tsave_off, x, b, d.elim,
             d.elim_ptr, d.bnd, d.bnd_ptr, d.f_ne, d.f_nb, L.first, L.n, L.E, r0, r1, c0, c1, cols, from_x); gbmhd::count_launch(); }
     }
     MF_CUDA(cudaGetLastError());
@@ -2572,22 +2583,42 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     return 0;
   };
   int rc = 0;
+  // Levels of several super-blocks (FP32 factors with TMA maps): the GEMV of super-block j is
+  // split into the next super-block's rows, which the next chain needs, and the rows beyond,
+  // which run on the second stream beside that chain and join before chain j + 2.  (Their
+  // partial sums are added atomically, so the two may overlap in their output rows.)
+  size_t evn = 0;
+  auto next_ev = [&]() { return M->sev[evn++ % M->sev.size()]; };
   for (size_t l = 0; l < S.levels.size(); ++l) {  // forward, bottom-up
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count, n = L.n, E = L.E;
     const bool wide = cnt >= 2 * ctx->num_sms;  // many fronts: small CTAs, one wave
-    for (int s0 = 0; s0 < E; s0 += SB) {
+    const bool split = !tr && sizeof(T) == 4 && M->map_ok[l] && M->cmap_ok[l] && E > SB;
+    cudaEvent_t rest_done[2] = {nullptr, nullptr};  // the row GEMVs beyond of super-blocks j − 2, j − 1
+    for (int s0 = 0, j = 0; s0 < E; s0 += SB, ++j) {
       const int s1 = std::min(E, s0 + SB);
       const int gather = s0 == 0;  // the first chain reads t = b[elim] for the whole front
       if (!tr) {
         constexpr int R = RowVec<T>::R;
+        if (split && rest_done[j & 1]) MF_CUDA(cudaStreamWaitEvent(ctx->stream, rest_done[j & 1], 0));
         if (sizeof(T) == 4 && M->cmap_ok[l]) {
           if ((rc = chain_tma(ctx, M, l, true, s0, s1, gather, b, x))) return rc;
         } else if (sizeof(T) == 8 || wide)
           { k_tri_fwd<T, 1><<<cnt, SB / R, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
         else
           { k_tri_fwd<T, TRI_G(4)><<<cnt, SB / R * TRI_G(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
-        if ((rc = rect(l, 0, s1, n, s0, s1, 0))) return rc;
+        if (split && s1 < E) {
+          const int s1n = std::min(E, s1 + SB);
+          cudaEvent_t ec = next_ev(), eb = next_ev();
+          MF_CUDA(cudaEventRecord(ec, ctx->stream));
+          MF_CUDA(cudaStreamWaitEvent(M->s2, ec, 0));
+          if ((rc = rect(l, 0, s1n, n, s0, s1, 0, M->s2))) return rc;
+          MF_CUDA(cudaEventRecord(eb, M->s2));
+          rest_done[j & 1] = eb;
+          if ((rc = rect(l, 0, s1, s1n, s0, s1, 0))) return rc;
+        } else {
+          if ((rc = rect(l, 0, s1, n, s0, s1, 0))) return rc;
+        }
       } else {
         if (sizeof(T) == 4 && M->cmap_ok[l]) {
           if ((rc = chain_tma_t(ctx, M, l, true, s0, s1, gather, b, x))) return rc;
@@ -2596,16 +2627,41 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
         if ((rc = rect_t(l, s0, s1, s1, n, 0))) return rc;
       }
     }
+    for (cudaEvent_t e : rest_done)  // join the second stream before the next level
+      if (e) MF_CUDA(cudaStreamWaitEvent(ctx->stream, e, 0));
     MF_CUDA(cudaGetLastError());
   }
   for (int l = (int)S.levels.size() - 1; l >= 0; --l) {  // backward, top-down
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count, n = L.n, E = L.E;
     const int nsb = (E + SB - 1) / SB;
+    // Backward split (as forward): the GEMV of super-block sb over the columns beyond
+    // super-block sb + 1 needs the x of super-blocks ≥ sb + 2 only, so it runs on the second
+    // stream after chain sb + 2 (the boundary columns: from the start of the level); the
+    // columns of super-block sb + 1 follow chain sb + 1 on the main stream.
+    const bool split = !tr && sizeof(T) == 4 && M->map_ok[l] && M->cmap_ok[l] && nsb >= 2;
+    std::vector<cudaEvent_t> rest_done(split ? nsb : 0, nullptr);
+    auto launch_rest = [&](int sb) -> int {  // columns [start of super-block sb + 2, n) of the rows of sb
+      const int r0 = sb * SB, r1 = std::min(E, r0 + SB), c0 = std::min(E, r1 + SB);
+      cudaEvent_t ec = next_ev(), eb = next_ev();
+      MF_CUDA(cudaEventRecord(ec, ctx->stream));
+      MF_CUDA(cudaStreamWaitEvent(M->s2, ec, 0));
+      const int rc2 = rect((size_t)l, 1, r0, r1, c0, n, 1, M->s2);
+      if (rc2) return rc2;
+      MF_CUDA(cudaEventRecord(eb, M->s2));
+      rest_done[sb] = eb;
+      return 0;
+    };
+    if (split && (rc = launch_rest(nsb - 2))) return rc;
     for (int sb = nsb - 1; sb >= 0; --sb) {
       const int s0 = sb * SB, s1 = std::min(E, s0 + SB);
       if (!tr) {
-        if ((rc = rect((size_t)l, 1, s0, s1, s1, n, 1))) return rc;
+        if (split && sb < nsb - 1) {
+          if ((rc = rect((size_t)l, 1, s0, s1, s1, std::min(E, s1 + SB), 1))) return rc;
+          MF_CUDA(cudaStreamWaitEvent(ctx->stream, rest_done[sb], 0));
+        } else {
+          if ((rc = rect((size_t)l, 1, s0, s1, s1, n, 1))) return rc;
+        }
         constexpr int W1 = 32 * NB / RowVec<T>::R / 4;  // threads of one column-group set
         if (sizeof(T) == 4 && M->cmap_ok[l]) {
           if ((rc = chain_tma(ctx, M, l, false, s0, s1, 0, b, x))) return rc;
@@ -2613,6 +2669,7 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
           { k_tri_bwd<T, 1><<<cnt, W1, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
         else
           { k_tri_bwd<T, TRI_GH(4)><<<cnt, W1 * TRI_GH(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+        if (split && sb >= 2 && (rc = launch_rest(sb - 2))) return rc;
       } else {
         if ((rc = rect_t((size_t)l, s1, n, s0, s1, 1))) return rc;
         if (sizeof(T) == 4 && M->cmap_ok[l]) {

@@ -22,6 +22,7 @@ SHAPES = [  # m, n, k, batch, alpha, beta
     (700, 650, 128, 2, -1.0, 1.0),
     (129, 257, 8, 1, -1.0, 1.0),
     (384, 384, 72, 4, -1.0, 1.0),
+    (2048, 2048, 128, 4, -1.0, 1.0),  # a trailing update of the size of a top-level front
 ]
 
 
