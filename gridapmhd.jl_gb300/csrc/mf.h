@@ -63,10 +63,11 @@ struct MFSymbolic {
 };
 
 // cell_row: [ncells][129] global free ids (-1 Dirichlet); uj_slot(a) selects the
-// local slots of u and j.  rowptr/col: CSR pattern of the full Jacobian.
+// local slots of u and j.  rowptr/col: CSR pattern of the full Jacobian.  order: the field
+// order of elimination inside each front, letters u, p, j, f (φ) (null: "jufp").
 std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t* cell_row, int64_t ndofs,
                        const int64_t* rowptr, const int32_t* col, bool monolithic, MFSymbolic& S,
-                       int leaf_cells = 8);
+                       int leaf_cells = 8, const char* order = nullptr);
 
 }  // namespace gbmhd
 

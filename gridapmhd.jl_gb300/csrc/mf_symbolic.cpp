@@ -25,7 +25,7 @@ inline int field_of_slot(int a) { return a < OP ? 0 : (a < OJ ? 1 : (a < OPHI ? 
 
 std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t* cell_row, int64_t ndofs,
                        const int64_t* rowptr, const int32_t* col, bool monolithic, MFSymbolic& S,
-                       int leaf_cells) {
+                       int leaf_cells, const char* order) {
   S = MFSymbolic();
   S.monolithic = monolithic;
   auto in_slot = [&](int a) { return monolithic || is_uj_slot(a); };
@@ -40,10 +40,11 @@ std::string mf_analyse(int64_t ncells, const double* cell_coords, const int32_t*
   for (int64_t d = 0; d < ndofs; ++d) S.nuj += is_uj[d];
   // Field order of elimination inside each front (u=0, p=1, j=2, φ=3 ranks).
   int field_rank[4] = {1, 3, 0, 2};  // j, u, φ, p
-  if (const char* o = std::getenv("GBMHD_ELIM_ORDER")) {
+  if (const char* o = std::getenv("GBMHD_ELIM_ORDER")) order = o;  // diagnostic override
+  if (order) {
     // e.g. "jufp": letters in elimination order
-    for (int i = 0; o[i] && i < 4; ++i) {
-      const int f = o[i] == 'u' ? 0 : o[i] == 'p' ? 1 : o[i] == 'j' ? 2 : 3;
+    for (int i = 0; order[i] && i < 4; ++i) {
+      const int f = order[i] == 'u' ? 0 : order[i] == 'p' ? 1 : order[i] == 'j' ? 2 : 3;
       field_rank[f] = i;
     }
   }

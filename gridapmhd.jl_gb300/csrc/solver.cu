@@ -25,6 +25,7 @@ using namespace gbmhd;
 struct Solver {
   MFNumeric* mf = nullptr;
   int pc_kind = -1;             // GBMHD_PC_MONOLITHIC or GBMHD_PC_BADIA2024
+  std::string mf_order;         // field order of elimination of the current symbolic analysis
   double* reg = nullptr;        // [ndofs] diagonal regularisation of the p and φ pivots
   double reg_eps = -1.0;
   bool have_mass = false;
@@ -419,11 +420,22 @@ static int ensure_workspace(gbmhd_ctx* ctx, int m) {
   return 0;
 }
 
+// Scale of the root regularisation −ε·diag(mass) of the global p/φ representatives for FP32
+// factors (FP64: 1).  Measured at 64×64×4, Ha = 500 (FGMRES iterations per Newton solve, order
+// u, j, φ, p): ε = 1: ~29; 1e-2: 25–28; 1e-3: 15–17; 1e-4: 15–16; 1e-5: a singular pivot block.
+constexpr double kEps32 = 1e-3;
+
 // Preconditioner set-up: (u,j) factorization + mass blocks.
 static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
   auto t0 = std::chrono::steady_clock::now();
   Solver* s = ctx->solver;
-  if (s->mf && s->pc_kind != kind) {
+  // Field order of elimination inside a front, per factor precision (measured at 64×64×4,
+  // Ha = 500, with the root regularisation below): FP32 factors precondition best with the
+  // velocities first (u, j, φ, p: 15–17 FGMRES iterations per Newton solve, against 80–87 for
+  // j, u, φ, p with ε = 1 and 27 with ε = 1e-3); with FP64 factors that order let the Newton
+  // residual drift up from its floor at the third step, so they keep j, u, φ, p.
+  const char* order = precision == GBMHD_FP64 ? "jufp" : "ujfp";
+  if (s->mf && (s->pc_kind != kind || s->mf_order != order)) {
     mf_destroy(s->mf);
     s->mf = nullptr;
   }
@@ -431,7 +443,8 @@ static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
   if (!s->mf) {
     MFSymbolic S;
     std::string e = mf_analyse(ctx->ncells, ctx->h_cellX.data(), ctx->h_cell_row.data(), ctx->ndofs,
-                               ctx->h_rowptr.data(), ctx->h_col.data(), kind == GBMHD_PC_MONOLITHIC, S);
+                               ctx->h_rowptr.data(), ctx->h_col.data(), kind == GBMHD_PC_MONOLITHIC, S, 8, order);
+    s->mf_order = order;
     if (!e.empty()) { ctx->err = e; return -1; }
     int rc = mf_create(ctx, S, &s->mf);
     if (rc) return rc;
@@ -452,7 +465,7 @@ static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
     S_CUDA(cudaMalloc(&s->seg, sizeof(int32_t) * 2 * ctx->ndofs));
     S_CUDA(cudaMemcpy(s->seg, seg.data(), sizeof(int32_t) * 2 * ctx->ndofs, cudaMemcpyHostToDevice));
   }
-  const double want_eps = precision == GBMHD_MIXED ? (std::getenv("GBMHD_PC_EPS32") ? std::atof(std::getenv("GBMHD_PC_EPS32")) : 1.0)
+  const double want_eps = precision == GBMHD_MIXED ? (std::getenv("GBMHD_PC_EPS32") ? std::atof(std::getenv("GBMHD_PC_EPS32")) : kEps32)
                                                    : (std::getenv("GBMHD_PC_EPS64") ? std::atof(std::getenv("GBMHD_PC_EPS64")) : 1.0);
   if (!s->have_mass || s->mass_beta != ctx->prm.beta || s->mass_zu != ctx->prm.zeta_u ||
       s->mass_zj != ctx->prm.zeta_j || s->reg_eps != want_eps) {
@@ -483,7 +496,7 @@ static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
     const double af = -1.0 / (1.0 + ctx->prm.zeta_j);
     // monolithic: the root's global p/φ representatives get −ε·diag(mass) scaled like the
     // Schur complements (only those pivots are singular when the walls fix u and j·n everywhere)
-    double eps = 1.0;
+    double eps = precision == GBMHD_MIXED ? kEps32 : 1.0;
     if (const char* ev = std::getenv(precision == GBMHD_MIXED ? "GBMHD_PC_EPS32" : "GBMHD_PC_EPS64")) eps = std::atof(ev);
     if (!s->reg) S_CUDA(cudaMalloc(&s->reg, sizeof(double) * ctx->ndofs));
     S_CUDA(cudaMemsetAsync(s->reg, 0, sizeof(double) * ctx->ndofs, ctx->stream));

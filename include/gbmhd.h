@@ -243,8 +243,9 @@ int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double*
  * library's behaviour is fixed.  They exist for measurements and for tests that drive
  * rarely taken paths on purpose.
  *   GBMHD_PC_EPS32, GBMHD_PC_EPS64  scale of the root's −ε·diag(mass) regularisation of the
- *                                   global p and φ pivots (FP32 / FP64 factors; default 1)
- *   GBMHD_ELIM_ORDER                field order of elimination inside a front (default "jufp")
+ *                                   global p and φ pivots (FP32 factors: default 1e-3; FP64: 1)
+ *   GBMHD_ELIM_ORDER                field order of elimination inside a front, both precisions
+ *                                   (default "ujfp" for FP32 factors, "jufp" for FP64)
  *   GBMHD_STAG_ITERS, GBMHD_STAG_REL  the mixed-precision stagnation test: a linear solve
  *                                   that has run GBMHD_STAG_ITERS iterations (default 100) with
  *                                   its relative residual still above GBMHD_STAG_REL (default
