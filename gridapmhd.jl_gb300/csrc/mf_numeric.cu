@@ -2,6 +2,8 @@
 #include <cublas_v2.h>
 #include <cuda.h>  // CUtensorMap types; the encoder is reached through the runtime's driver entry point
 
+#include <chrono>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <utility>
@@ -85,6 +87,11 @@ struct MFNumeric {
   // second stream of the sweeps: the GEMVs beyond the next super-block run beside the chains
   cudaStream_t s2 = nullptr;
   std::vector<cudaEvent_t> sev;      // a pool of events for the fork/join points of a solve
+  // the level groups of one tree height run side by side in a solve: branch streams, their
+  // fork/join events and the tree height of each level
+  std::vector<cudaStream_t> bstreams;
+  std::vector<cudaEvent_t> fev;
+  std::vector<int32_t> lheight;
   bool ev_pending = false;
   int64_t sweep_applies = 0;
   double sweep_seconds = 0.0;
@@ -196,6 +203,26 @@ int mf_create(gbmhd_ctx* ctx, const MFSymbolic& S, MFNumeric** out) {
   MF_CUDA(cudaStreamCreateWithFlags(&M->s2, cudaStreamNonBlocking));
   M->sev.assign(64, nullptr);
   for (cudaEvent_t& e : M->sev) MF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  {
+    // tree height of every front (a parent follows its children in the front order), and the
+    // widest run of levels of one height
+    std::vector<int32_t> fh(S.f_ne.size(), 0);
+    for (size_t f = 0; f < fh.size(); ++f)
+      if (S.f_parent[f] >= 0) fh[S.f_parent[f]] = std::max(fh[S.f_parent[f]], fh[f] + 1);
+    M->lheight.resize(S.levels.size());
+    size_t widest = 1, run = 0;
+    for (size_t l = 0; l < S.levels.size(); ++l) {
+      M->lheight[l] = S.levels[l].count > 0 ? fh[S.levels[l].first] : -1;
+      run = (l > 0 && M->lheight[l] == M->lheight[l - 1]) ? run + 1 : 1;
+      widest = std::max(widest, run);
+    }
+    if (const char* bs = std::getenv("GBMHD_SWEEP_BRANCHES"))  // 0: levels one by one
+      if (std::atoi(bs) == 0) widest = 1;
+    M->bstreams.assign(std::min<size_t>(widest - 1, 7), nullptr);
+    for (cudaStream_t& st : M->bstreams) MF_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    M->fev.assign(16, nullptr);
+    for (cudaEvent_t& e : M->fev) MF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
   if ((rc = upload(ctx, &M->tsave_off, toff))) return rc;
   MF_CUDA(cudaMalloc(&M->tsave, sizeof(double) * std::max<int64_t>(t, 1)));
   MF_CUDA(cudaMalloc(&M->d_err, sizeof(int32_t)));
@@ -233,6 +260,10 @@ void mf_destroy(MFNumeric* M) {
   if (M->ev1) cudaEventDestroy(M->ev1);
   for (cudaEvent_t e : M->sev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : M->fev)
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t st : M->bstreams)
+    if (st) cudaStreamDestroy(st);
   if (M->s2) cudaStreamDestroy(M->s2);
   delete M;
 }
@@ -626,6 +657,140 @@ __global__ void __launch_bounds__(NB * CGN) k_pivot_inverse_df(const float* __re
   __syncthreads();
   float* Pf = P + f * (int64_t)NB * NB;
   for (int j = tj; j < NB; j += CGN)  // column-major, zero outside kb x kb
+    Pf[ti + j * NB] = (ti < kb && j < kb) ? Ob[ti + colsrc[j] * LD] : 0.0f;
+}
+
+// The same Gauss-Jordan steps with one barrier per column step.  Warp w holds columns w and
+// w + 32 of the block, lane l rows l and l + 32 (four float-float entries per thread), so
+// that a column lies in one warp and the pivot row's and row c's entries of a warp's columns
+// lie in its own lanes.  The warp that holds column c + 1 updates it in step c, then at once
+// searches its pivot and publishes (double-buffered in shared memory) the pivot row, the
+// float-float reciprocal of the pivot and the multipliers m_i = A[i, c + 1] after the
+// interchange; after the step's one barrier every warp forms its own entries of the scaled
+// pivot row with warp shuffles.  Every entry goes through the same operations, in the same
+// order, as in k_pivot_inverse_df, so the two kernels give the same bits.
+__global__ void __launch_bounds__(1024) k_pivot_inverse_dfw(const float* __restrict__ F, int64_t off, int n, int k,
+                                                           int kb, float* __restrict__ P, int32_t* err) {
+  constexpr int LD = NB + 1;
+  __shared__ float Ob[NB * LD];
+  __shared__ float mh[2][NB], ml[2][NB];
+  __shared__ float sih[2], sil[2];
+  __shared__ int spr[2];
+  __shared__ int perm[NB], colsrc[NB];
+  const int64_t f = blockIdx.x;
+  const float* M = F + off + f * (int64_t)n * n;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  constexpr unsigned FULL = 0xffffffffu;
+  float h[2][2], l[2][2];  // [s][q]: column w + 32 s, row lane + 32 q
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int i = lane + 32 * q, j = w + 32 * s;
+      h[s][q] = (i < kb && j < kb) ? M[(k + i) + (int64_t)(k + j) * n] : 0.0f;
+      l[s][q] = 0.0f;
+    }
+  // the warp holding column c: pivot row (argmax of the high parts over rows c..kb-1, ties:
+  // the lower row), 1 / pivot and the multipliers into buffer c & 1
+  auto publish = [&](int c) {
+    const int sc = c >> 5, b = c & 1;
+    float vh[2], vl[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      vh[q] = sc ? h[1][q] : h[0][q];
+      vl[q] = sc ? l[1][q] : l[0][q];
+    }
+    float best = (lane >= c && lane < kb) ? fabsf(vh[0]) : -1.0f;
+    int bi = lane;
+    if (lane + 32 >= c && lane + 32 < kb && fabsf(vh[1]) > best) { best = fabsf(vh[1]); bi = lane + 32; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ob = __shfl_xor_sync(FULL, best, o);
+      const int oi = __shfl_xor_sync(FULL, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const int pr = best > 0.0f ? bi : c;  // singular block: keep going, the error flag is set
+    const float dh = __shfl_sync(FULL, (pr >> 5) ? vh[1] : vh[0], pr & 31);
+    const float dl = __shfl_sync(FULL, (pr >> 5) ? vl[1] : vl[0], pr & 31);
+    const float ch_ = __shfl_sync(FULL, (c >> 5) ? vh[1] : vh[0], c & 31);  // A[c, c]
+    const float cl_ = __shfl_sync(FULL, (c >> 5) ? vl[1] : vl[0], c & 31);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int i = lane + 32 * q;
+      float m_h = vh[q], m_l = vl[q];
+      if (i == pr) { m_h = ch_; m_l = cl_; }  // row pr now holds the old row c
+      if (i == c) { m_h = 0.0f; m_l = 0.0f; }
+      mh[b][i] = m_h;
+      ml[b][i] = m_l;
+    }
+    if (lane == 0) {
+      float ih = 0.0f, il = 0.0f;
+      if (dh != 0.0f) df_rcp(dh, dl, ih, il);
+      sih[b] = ih;
+      sil[b] = il;
+      spr[b] = pr;
+      perm[c] = pr;
+      if (!(best > 0.0f)) atomicExch(err, 1);
+    }
+  };
+  if (w == 0 && kb > 0) publish(0);
+  __syncthreads();
+  for (int c = 0; c < kb; ++c) {
+    const int b = c & 1;
+    const int pr = spr[b];
+    const float ih = sih[b], il = sil[b];
+    const bool swap = pr != c;
+    float m_h[2], m_l[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      m_h[q] = mh[b][lane + 32 * q];
+      m_l[q] = ml[b][lane + 32 * q];
+    }
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int j = w + 32 * s;
+      // the pivot row's and the old row c's entries of column j
+      const float ah_p = __shfl_sync(FULL, (pr >> 5) ? h[s][1] : h[s][0], pr & 31);
+      const float al_p = __shfl_sync(FULL, (pr >> 5) ? l[s][1] : l[s][0], pr & 31);
+      const float ah_c = __shfl_sync(FULL, (c >> 5) ? h[s][1] : h[s][0], c & 31);
+      const float al_c = __shfl_sync(FULL, (c >> 5) ? l[s][1] : l[s][0], c & 31);
+      float r_h, r_l;
+      if (j == c) { r_h = ih; r_l = il; }
+      else df_mul(ah_p, al_p, ih, il, r_h, r_l);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int i = lane + 32 * q;
+        if (i == c) {
+          h[s][q] = r_h;
+          l[s][q] = r_l;
+        } else {
+          const bool from_c = swap && i == pr;
+          float ah = from_c ? ah_c : h[s][q], al = from_c ? al_c : l[s][q];
+          if (j == c) { ah = 0.0f; al = 0.0f; }
+          df_sub_prod(ah, al, m_h[q], m_l[q], r_h, r_l, h[s][q], l[s][q]);
+        }
+      }
+    }
+    if (c + 1 < kb && w == ((c + 1) & 31)) publish(c + 1);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int q = 0; q < 2; ++q) Ob[(lane + 32 * q) + (w + 32 * s) * LD] = __fadd_rn(h[s][q], l[s][q]);
+  if (threadIdx.x == 0) {  // undo the row interchanges as column interchanges, last first
+    for (int j = 0; j < kb; ++j) colsrc[j] = j;
+    for (int c = kb - 1; c >= 0; --c) {
+      const int p = perm[c];
+      const int t = colsrc[c];
+      colsrc[c] = colsrc[p];
+      colsrc[p] = t;
+    }
+  }
+  __syncthreads();
+  float* Pf = P + f * (int64_t)NB * NB;
+  const int ti = threadIdx.x & (NB - 1), tj = threadIdx.x >> 6;
+  for (int j = tj; j < NB; j += 16)  // column-major, zero outside kb x kb
     Pf[ti + j * NB] = (ti < kb && j < kb) ? Ob[ti + colsrc[j] * LD] : 0.0f;
 }
 
@@ -2171,6 +2336,26 @@ static int gemm(gbmhd_ctx* ctx, MFNumeric* M, int m, int n, int k, T alpha, cons
   }
 }
 
+// Pivot-block inverse of the FP32 factors: 0 = k_pivot_inverse_df<16>, 1 = k_pivot_inverse_df<4>,
+// 2 = k_pivot_inverse_df_smem, 3 = k_pivot_inverse_dfw.  All four give the same bits.
+static void launch_pivot_inverse(int variant, int cnt, cudaStream_t st, const float* F, int64_t off, int n, int k,
+                                 int kb, float* P, int32_t* err) {
+  switch (variant) {
+    case 0: k_pivot_inverse_df<16><<<cnt, NB * 16, 0, st>>>(F, off, n, k, kb, P, err); break;
+    case 1: k_pivot_inverse_df<4><<<cnt, NB * 4, 0, st>>>(F, off, n, k, kb, P, err); break;
+    case 2: k_pivot_inverse_df_smem<<<cnt, 256, 0, st>>>(F, off, n, k, kb, P, err); break;
+    default: k_pivot_inverse_dfw<<<cnt, 1024, 0, st>>>(F, off, n, k, kb, P, err); break;
+  }
+}
+
+// forced: the GBMHD_PIVOT_KERNEL override (-1: none).  Measured on one GB300 (64 x 64 blocks,
+// per launch): 1–152 blocks 98 µs (0), 156 µs (1), 133 µs (2), 84 µs (3); 256 blocks 193, 177,
+// 150, 142 µs; 2048 blocks 1333, 964, 666, 907 µs.
+static int pivot_variant(const gbmhd_ctx* ctx, int cnt, int forced) {
+  if (forced >= 0 && forced <= 3) return forced;
+  return cnt >= 2 * ctx->num_sms ? 2 : 3;
+}
+
 template <typename T, typename V>
 static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double* d_reg) {
   const MFSymbolic& S = M->S;
@@ -2226,9 +2411,25 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
   MF_CUDA(cudaMemcpyAsync(d_ln, ln.data(), sizeof(int) * ln.size(), cudaMemcpyHostToDevice, ctx->stream));
   MF_CUDA(cudaMemcpyAsync(d_le, le.data(), sizeof(int) * le.size(), cudaMemcpyHostToDevice, ctx->stream));
   const T one = 1, mone = -1, zero = 0;
+  const char* pks = std::getenv("GBMHD_PIVOT_KERNEL");
+  const int pk = pks ? std::atoi(pks) : -1;
+  // GBMHD_MF_LEVEL_TIMES: device time of each level (CUDA events) and the host's time to
+  // issue it, printed to stderr
+  const bool ltimes = std::getenv("GBMHD_MF_LEVEL_TIMES") != nullptr;
+  std::vector<cudaEvent_t> lev_ev;
+  std::vector<double> lev_host;
+  if (ltimes) {
+    lev_ev.resize(S.levels.size() + 1);
+    for (cudaEvent_t& e : lev_ev) MF_CUDA(cudaEventCreate(&e));
+    lev_host.resize(S.levels.size() + 1);
+  }
   for (size_t l = 0; l < S.levels.size(); ++l) {
     const MFLevel& L = S.levels[l];
     const int n = L.n, E = L.E;
+    if (ltimes) {
+      MF_CUDA(cudaEventRecord(lev_ev[l], ctx->stream));
+      lev_host[l] = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+    }
     const int cnt = (int)L.count;
     const long long sn = (long long)n * n;  // front stride
     T* F0 = F + L.off;
@@ -2265,9 +2466,7 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
         const int kb = std::min(NB, p + pw - k);
         if constexpr (sizeof(T) == 4)
           {
-            if (cnt >= 2 * ctx->num_sms) k_pivot_inverse_df_smem<<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err);
-            else if (cnt >= ctx->num_sms) k_pivot_inverse_df<4><<<cnt, NB * 4, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err);
-            else k_pivot_inverse_df<16><<<cnt, NB * 16, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err);
+            launch_pivot_inverse(pivot_variant(ctx, cnt, pk), cnt, ctx->stream, F, L.off, n, k, kb, P, M->d_err);
             gbmhd::count_launch();
           }
         else
@@ -2314,11 +2513,28 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
       }
     }
   }
+  if (ltimes) {
+    MF_CUDA(cudaEventRecord(lev_ev.back(), ctx->stream));
+    lev_host.back() = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  }
   MF_CUDA(cudaFreeAsync(d_ln, ctx->stream));
   MF_CUDA(cudaFreeAsync(d_le, ctx->stream));
   int32_t herr = 0;
   MF_CUDA(cudaMemcpyAsync(&herr, M->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
   MF_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (ltimes) {
+    double dev_total = 0.0;
+    for (size_t l = 0; l < S.levels.size(); ++l) {
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, lev_ev[l], lev_ev[l + 1]);
+      dev_total += ms;
+      std::fprintf(stderr, "mf level %2zu: fronts %6lld E %5d n %5d  device %8.3f ms  host issue %8.3f ms\n", l,
+                   (long long)S.levels[l].count, S.levels[l].E, S.levels[l].n, ms,
+                   1e3 * (lev_host[l + 1] - lev_host[l]));
+    }
+    std::fprintf(stderr, "mf levels: device %.3f ms (precision %d, pivot kernel %d)\n", dev_total, (int)sizeof(T), pk);
+    for (cudaEvent_t e : lev_ev) cudaEventDestroy(e);
+  }
   if (herr) {
     ctx->err = herr == 2 ? "multifrontal: a tensor-core GEMM wait timed out"
                          : "multifrontal: singular pivot block in the factorization";
@@ -2450,21 +2666,21 @@ static cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
 // the ring a step and a half ahead).
 template <int G, int NS>
 static int chain_launch(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0, int s1, int gather,
-                        const double* b, double* x) {
+                        const double* b, double* x, cudaStream_t st) {
   const MFLevel& L = M->S.levels[l];
   const DevSym& d = M->d;
   const int sm = NS * CH_BOX_BYTES;
   if (fwd) {
     MF_CUDA(cudaFuncSetAttribute(k_chain_fwd<G, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     MF_CUDA(cudaFuncSetAttribute(k_chain_fwd<G, NS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    MF_CUDA(launch_pdl(k_chain_fwd<G, NS>, dim3((unsigned)L.count), dim3(128 * G), sm, ctx->stream, M->cmaps[l],
+    MF_CUDA(launch_pdl(k_chain_fwd<G, NS>, dim3((unsigned)L.count), dim3(128 * G), sm, st, M->cmaps[l],
                        L.first, M->tsave, (const int64_t*)M->tsave_off, b, (const int32_t*)d.elim,
                        (const int64_t*)d.elim_ptr, (const int32_t*)d.f_ne, L.E, s0, s1, gather, M->d_sweep_err,
                        M->wait_limit));
   } else {
     MF_CUDA(cudaFuncSetAttribute(k_chain_bwd<G, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     MF_CUDA(cudaFuncSetAttribute(k_chain_bwd<G, NS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    MF_CUDA(launch_pdl(k_chain_bwd<G, NS>, dim3((unsigned)L.count), dim3(128 * G), sm, ctx->stream, M->cmaps[l],
+    MF_CUDA(launch_pdl(k_chain_bwd<G, NS>, dim3((unsigned)L.count), dim3(128 * G), sm, st, M->cmaps[l],
                        L.first, (const double*)M->tsave, (const int64_t*)M->tsave_off, x, (const int32_t*)d.elim,
                        (const int64_t*)d.elim_ptr, (const int32_t*)d.f_ne, s0, s1, M->d_sweep_err,
                        M->wait_limit));
@@ -2513,14 +2729,14 @@ static int chain_tma_t(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0,
 }
 
 static int chain_tma(gbmhd_ctx* ctx, MFNumeric* M, size_t l, bool fwd, int s0, int s1, int gather, const double* b,
-                     double* x) {
+                     double* x, cudaStream_t st) {
   const int nb = (s1 - s0 + NB - 1) / NB;
   if (M->S.levels[l].count >= 2 * ctx->num_sms) {
-    if (nb <= 4) return chain_launch<1, 4>(ctx, M, l, fwd, s0, s1, gather, b, x);
-    if (nb <= 6) return chain_launch<1, 6>(ctx, M, l, fwd, s0, s1, gather, b, x);
-    return chain_launch<1, 8>(ctx, M, l, fwd, s0, s1, gather, b, x);
+    if (nb <= 4) return chain_launch<1, 4>(ctx, M, l, fwd, s0, s1, gather, b, x, st);
+    if (nb <= 6) return chain_launch<1, 6>(ctx, M, l, fwd, s0, s1, gather, b, x, st);
+    return chain_launch<1, 8>(ctx, M, l, fwd, s0, s1, gather, b, x, st);
   }
-  return chain_launch<4, 12>(ctx, M, l, fwd, s0, s1, gather, b, x);
+  return chain_launch<4, 12>(ctx, M, l, fwd, s0, s1, gather, b, x, st);
 }
 
 // One application of the factors: x = A⁻¹ b (or A⁻ᵀ b when tr) on the factorized dofs.  Per
@@ -2589,35 +2805,36 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
   // partial sums are added atomically, so the two may overlap in their output rows.)
   size_t evn = 0;
   auto next_ev = [&]() { return M->sev[evn++ % M->sev.size()]; };
-  for (size_t l = 0; l < S.levels.size(); ++l) {  // forward, bottom-up
+  // forward substitution of level l on stream st (the split GEMVs only on the context stream)
+  auto fwd_level = [&](size_t l, cudaStream_t st) -> int {
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count, n = L.n, E = L.E;
     const bool wide = cnt >= 2 * ctx->num_sms;  // many fronts: small CTAs, one wave
-    const bool split = !tr && sizeof(T) == 4 && M->map_ok[l] && M->cmap_ok[l] && E > SB;
+    const bool split = st == ctx->stream && !tr && sizeof(T) == 4 && M->map_ok[l] && M->cmap_ok[l] && E > SB;
     cudaEvent_t rest_done[2] = {nullptr, nullptr};  // the row GEMVs beyond of super-blocks j − 2, j − 1
     for (int s0 = 0, j = 0; s0 < E; s0 += SB, ++j) {
       const int s1 = std::min(E, s0 + SB);
       const int gather = s0 == 0;  // the first chain reads t = b[elim] for the whole front
       if (!tr) {
         constexpr int R = RowVec<T>::R;
-        if (split && rest_done[j & 1]) MF_CUDA(cudaStreamWaitEvent(ctx->stream, rest_done[j & 1], 0));
+        if (split && rest_done[j & 1]) MF_CUDA(cudaStreamWaitEvent(st, rest_done[j & 1], 0));
         if (sizeof(T) == 4 && M->cmap_ok[l]) {
-          if ((rc = chain_tma(ctx, M, l, true, s0, s1, gather, b, x))) return rc;
+          if ((rc = chain_tma(ctx, M, l, true, s0, s1, gather, b, x, st))) return rc;
         } else if (sizeof(T) == 8 || wide)
-          { k_tri_fwd<T, 1><<<cnt, SB / R, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
+          { k_tri_fwd<T, 1><<<cnt, SB / R, 0, st>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
         else
-          { k_tri_fwd<T, TRI_G(4)><<<cnt, SB / R * TRI_G(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
+          { k_tri_fwd<T, TRI_G(4)><<<cnt, SB / R * TRI_G(4), 0, st>>>(F, d.f_off, M->tsave, M->tsave_off, b, d.elim, d.elim_ptr, d.f_ne, L.first, n, E, s0, s1, gather); gbmhd::count_launch(); }
         if (split && s1 < E) {
           const int s1n = std::min(E, s1 + SB);
           cudaEvent_t ec = next_ev(), eb = next_ev();
-          MF_CUDA(cudaEventRecord(ec, ctx->stream));
+          MF_CUDA(cudaEventRecord(ec, st));
           MF_CUDA(cudaStreamWaitEvent(M->s2, ec, 0));
           if ((rc = rect(l, 0, s1n, n, s0, s1, 0, M->s2))) return rc;
           MF_CUDA(cudaEventRecord(eb, M->s2));
           rest_done[j & 1] = eb;
-          if ((rc = rect(l, 0, s1, s1n, s0, s1, 0))) return rc;
+          if ((rc = rect(l, 0, s1, s1n, s0, s1, 0, st))) return rc;
         } else {
-          if ((rc = rect(l, 0, s1, n, s0, s1, 0))) return rc;
+          if ((rc = rect(l, 0, s1, n, s0, s1, 0, st))) return rc;
         }
       } else {
         if (sizeof(T) == 4 && M->cmap_ok[l]) {
@@ -2628,10 +2845,12 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       }
     }
     for (cudaEvent_t e : rest_done)  // join the second stream before the next level
-      if (e) MF_CUDA(cudaStreamWaitEvent(ctx->stream, e, 0));
+      if (e) MF_CUDA(cudaStreamWaitEvent(st, e, 0));
     MF_CUDA(cudaGetLastError());
-  }
-  for (int l = (int)S.levels.size() - 1; l >= 0; --l) {  // backward, top-down
+    return 0;
+  };
+  // backward substitution of level l on stream st
+  auto bwd_level = [&](size_t l, cudaStream_t st) -> int {
     const MFLevel& L = S.levels[l];
     const int cnt = (int)L.count, n = L.n, E = L.E;
     const int nsb = (E + SB - 1) / SB;
@@ -2639,14 +2858,14 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
     // super-block sb + 1 needs the x of super-blocks ≥ sb + 2 only, so it runs on the second
     // stream after chain sb + 2 (the boundary columns: from the start of the level); the
     // columns of super-block sb + 1 follow chain sb + 1 on the main stream.
-    const bool split = !tr && sizeof(T) == 4 && M->map_ok[l] && M->cmap_ok[l] && nsb >= 2;
+    const bool split = st == ctx->stream && !tr && sizeof(T) == 4 && M->map_ok[l] && M->cmap_ok[l] && nsb >= 2;
     std::vector<cudaEvent_t> rest_done(split ? nsb : 0, nullptr);
     auto launch_rest = [&](int sb) -> int {  // columns [start of super-block sb + 2, n) of the rows of sb
       const int r0 = sb * SB, r1 = std::min(E, r0 + SB), c0 = std::min(E, r1 + SB);
       cudaEvent_t ec = next_ev(), eb = next_ev();
-      MF_CUDA(cudaEventRecord(ec, ctx->stream));
+      MF_CUDA(cudaEventRecord(ec, st));
       MF_CUDA(cudaStreamWaitEvent(M->s2, ec, 0));
-      const int rc2 = rect((size_t)l, 1, r0, r1, c0, n, 1, M->s2);
+      const int rc2 = rect(l, 1, r0, r1, c0, n, 1, M->s2);
       if (rc2) return rc2;
       MF_CUDA(cudaEventRecord(eb, M->s2));
       rest_done[sb] = eb;
@@ -2657,21 +2876,21 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       const int s0 = sb * SB, s1 = std::min(E, s0 + SB);
       if (!tr) {
         if (split && sb < nsb - 1) {
-          if ((rc = rect((size_t)l, 1, s0, s1, s1, std::min(E, s1 + SB), 1))) return rc;
-          MF_CUDA(cudaStreamWaitEvent(ctx->stream, rest_done[sb], 0));
+          if ((rc = rect(l, 1, s0, s1, s1, std::min(E, s1 + SB), 1, st))) return rc;
+          MF_CUDA(cudaStreamWaitEvent(st, rest_done[sb], 0));
         } else {
-          if ((rc = rect((size_t)l, 1, s0, s1, s1, n, 1))) return rc;
+          if ((rc = rect(l, 1, s0, s1, s1, n, 1, st))) return rc;
         }
         constexpr int W1 = 32 * NB / RowVec<T>::R / 4;  // threads of one column-group set
         if (sizeof(T) == 4 && M->cmap_ok[l]) {
-          if ((rc = chain_tma(ctx, M, l, false, s0, s1, 0, b, x))) return rc;
+          if ((rc = chain_tma(ctx, M, l, false, s0, s1, 0, b, x, st))) return rc;
         } else if (cnt >= ctx->num_sms || sizeof(T) == 8)
-          { k_tri_bwd<T, 1><<<cnt, W1, 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+          { k_tri_bwd<T, 1><<<cnt, W1, 0, st>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
         else
-          { k_tri_bwd<T, TRI_GH(4)><<<cnt, W1 * TRI_GH(4), 0, ctx->stream>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
+          { k_tri_bwd<T, TRI_GH(4)><<<cnt, W1 * TRI_GH(4), 0, st>>>(F, d.f_off, M->tsave, M->tsave_off, x, d.elim, d.elim_ptr, d.f_ne, L.first, n, s0, s1); gbmhd::count_launch(); }
         if (split && sb >= 2 && (rc = launch_rest(sb - 2))) return rc;
       } else {
-        if ((rc = rect_t((size_t)l, s1, n, s0, s1, 1))) return rc;
+        if ((rc = rect_t(l, s1, n, s0, s1, 1))) return rc;
         if (sizeof(T) == 4 && M->cmap_ok[l]) {
           if ((rc = chain_tma_t(ctx, M, l, false, s0, s1, 0, b, x))) return rc;
         } else
@@ -2680,6 +2899,52 @@ static int solve_impl(gbmhd_ctx* ctx, MFNumeric* M, double* b, double* x, bool t
       }
     }
     MF_CUDA(cudaGetLastError());
+    return 0;
+  };
+  // The level groups of one tree height are independent in both substitutions: a group reads
+  // only the dofs its descendants (forward) or ancestors (backward) produce, writes its own
+  // eliminated dofs, and adds into its ancestors' boundary dofs atomically.  So the groups of
+  // one height run side by side: the first (the largest fronts) on the context stream, the
+  // others on the branch streams, joined before the next height.  The transposed solve
+  // shares one packing buffer between levels and keeps them in sequence.
+  size_t fvn = 0;
+  auto next_fev = [&]() { return M->fev[fvn++ % M->fev.size()]; };
+  auto run_height = [&](size_t la, size_t lb, bool fwd) -> int {  // levels [la, lb), one height
+    const bool conc = !tr && lb - la > 1 && !M->bstreams.empty();
+    if (!conc) {
+      for (size_t i = 0; i < lb - la; ++i) {
+        const size_t l = fwd ? la + i : lb - 1 - i;
+        if ((rc = fwd ? fwd_level(l, ctx->stream) : bwd_level(l, ctx->stream))) return rc;
+      }
+      return 0;
+    }
+    const size_t nbs = M->bstreams.size();
+    cudaEvent_t fork = next_fev();
+    MF_CUDA(cudaEventRecord(fork, ctx->stream));
+    for (size_t i = 1; i < lb - la && i <= nbs; ++i) MF_CUDA(cudaStreamWaitEvent(M->bstreams[i - 1], fork, 0));
+    for (size_t i = 0; i < lb - la; ++i) {
+      const cudaStream_t st = i == 0 ? ctx->stream : M->bstreams[(i - 1) % nbs];
+      if ((rc = fwd ? fwd_level(la + i, st) : bwd_level(la + i, st))) return rc;
+    }
+    for (size_t i = 1; i < lb - la && i <= nbs; ++i) {
+      cudaEvent_t join = next_fev();
+      MF_CUDA(cudaEventRecord(join, M->bstreams[i - 1]));
+      MF_CUDA(cudaStreamWaitEvent(ctx->stream, join, 0));
+    }
+    return 0;
+  };
+  const size_t nlev = S.levels.size();
+  for (size_t la = 0; la < nlev;) {  // forward, bottom-up
+    size_t lb = la + 1;
+    while (lb < nlev && M->lheight[lb] == M->lheight[la]) ++lb;
+    if ((rc = run_height(la, lb, true))) return rc;
+    la = lb;
+  }
+  for (size_t lb = nlev; lb > 0;) {  // backward, top-down
+    size_t la = lb - 1;
+    while (la > 0 && M->lheight[la - 1] == M->lheight[lb - 1]) --la;
+    if ((rc = run_height(la, lb, false))) return rc;
+    lb = la;
   }
   return 0;
 }
@@ -2771,4 +3036,38 @@ int mf_check_sweeps(gbmhd_ctx* ctx, MFNumeric* M) {
     return -3;
   }
   return 0;
+}
+
+extern "C" int gbmhd_diag_pivot_inverse(int32_t variant, int32_t count, int32_t n, int32_t kb, const float* F, float* P,
+                                        int32_t reps, double* ms_per_launch, int32_t* status) {
+  if (variant < 0 || variant > 3 || count < 1 || n < 1 || kb < 1 || kb > NB || kb > n || !F || !P || reps < 0)
+    return -1;
+  int32_t* d_err = nullptr;
+  if (cudaMalloc(&d_err, sizeof(int32_t)) != cudaSuccess) return -2;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = 0;
+  if (cudaMemset(d_err, 0, sizeof(int32_t)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess)
+    rc = -2;
+  if (!rc) {
+    launch_pivot_inverse(variant, count, nullptr, F, 0, n, 0, kb, P, d_err);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = -2;
+  }
+  int32_t h = 0;
+  if (!rc && cudaMemcpy(&h, d_err, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) rc = -2;
+  if (!rc && reps > 0) {
+    cudaEventRecord(e0, nullptr);
+    for (int r = 0; r < reps; ++r) launch_pivot_inverse(variant, count, nullptr, F, 0, n, 0, kb, P, d_err);
+    cudaEventRecord(e1, nullptr);
+    float ms = 0.0f;
+    if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      rc = -2;
+    if (ms_per_launch) *ms_per_launch = ms / reps;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(d_err);
+  if (status) *status = h;
+  return rc;
 }

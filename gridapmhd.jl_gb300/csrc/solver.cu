@@ -51,6 +51,11 @@ struct Solver {
   int64_t* permT = nullptr;
   double* valT = nullptr;
   int64_t factor_gen = -1;      // ctx->params_gen when the factors were computed
+  // constant-pressure mode: 1 when the all-ones vector on the p dofs is a null vector of the
+  // Jacobian (velocity fixed on every wall), checked once per parameter set
+  int p_null = -1;
+  int64_t p_null_gen = -1;
+  double* gsum = nullptr;       // [2] device scratch of the check and the projection
 };
 
 #define S_CUDA GB_CUDA
@@ -58,6 +63,48 @@ struct Solver {
 // Layout of Solver::hdev / hhost: [0, 256) first Gram–Schmidt pass, [256, 512) second
 // pass, [512] squared norm of the new direction.
 constexpr int kHB = 256, kHN = 512, kHcol = 513;
+
+// ---- the constant-pressure mode
+// max over rows of |Σ_c J[r, c]| and of Σ_c |J[r, c]| over the columns c in [cb, ce) (the p
+// dofs), as the bit patterns of non-negative doubles (which order like the values)
+__global__ void k_const_mode(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                             const double* __restrict__ val, int32_t cb, int32_t ce, unsigned long long* out) {
+  double sm = 0.0, am = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0, a = 0.0;
+    for (int64_t e = rowptr[r]; e < rowptr[r + 1]; ++e)
+      if (col[e] >= cb && col[e] < ce) {
+        s += val[e];
+        a += fabs(val[e]);
+      }
+    sm = fmax(sm, fabs(s));
+    am = fmax(am, a);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sm = fmax(sm, __shfl_xor_sync(0xffffffffu, sm, o));
+    am = fmax(am, __shfl_xor_sync(0xffffffffu, am, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&out[0], (unsigned long long)__double_as_longlong(sm));
+    atomicMax(&out[1], (unsigned long long)__double_as_longlong(am));
+  }
+}
+
+// out[0] += Σ_{i in [a, b)} v[i]
+__global__ void k_range_sum(const double* __restrict__ v, int64_t a, int64_t b, double* out) {
+  double s = 0.0;
+  for (int64_t i = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < b; i += (int64_t)gridDim.x * blockDim.x)
+    s += v[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+// v[i] −= sum / (b − a), i in [a, b)
+__global__ void k_range_shift(double* __restrict__ v, int64_t a, int64_t b, const double* __restrict__ sum) {
+  const double m = *sum / (double)(b - a);
+  for (int64_t i = a + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < b; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] -= m;
+}
 
 // ------------------------------------------------------------------ kernels
 // y = A x for the FP32 Jacobian: x arrives rounded to FP32 and the products accumulate in
@@ -426,6 +473,36 @@ static int ensure_workspace(gbmhd_ctx* ctx, int m) {
 constexpr double kEps32 = 1e-3;
 
 // Preconditioner set-up: (u,j) factorization + mass blocks.
+// Removes the constant-pressure component from a Newton update δ (δ_p −= mean δ_p) when the
+// all-ones vector on the p dofs is a null vector of the Jacobian: the pressure is then defined
+// up to a constant, and the preconditioner (whose root carries −ε·mass on the global p
+// representatives) amplifies that component of the residual's rounding by ~1/ε.  Left in
+// place, it lets the pressure level drift from step to step, and the rounding of the FP64
+// residual grows with it until Newton stalls above its tolerance.  J·1_p = 0, so the removal
+// changes no J·δ.  The null test uses the FP64 Jacobian (assembled before each Newton step):
+// max_r |Σ_p J[r, p]| ≤ 1e-10 · max_r Σ_p |J[r, p]|.
+static int project_pressure_gauge(gbmhd_ctx* ctx, double* delta) {
+  Solver* s = ctx->solver;
+  const int64_t pb = ctx->offs[1], pe = ctx->offs[2];
+  if (pe <= pb || !ctx->d_val64) return 0;
+  if (!s->gsum) S_CUDA(cudaMalloc(&s->gsum, 2 * sizeof(double)));
+  if (s->p_null < 0 || s->p_null_gen != ctx->params_gen) {
+    S_CUDA(cudaMemsetAsync(s->gsum, 0, 2 * sizeof(double), ctx->stream));
+    { k_const_mode<<<grid_for(ctx, ctx->ndofs), 256, 0, ctx->stream>>>(ctx->ndofs, ctx->d_rowptr, ctx->d_col, ctx->d_val64, (int32_t)pb, (int32_t)pe, reinterpret_cast<unsigned long long*>(s->gsum)); gbmhd::count_launch(); }
+    double h[2] = {0.0, 0.0};
+    S_CUDA(cudaMemcpyAsync(h, s->gsum, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    S_CUDA(cudaStreamSynchronize(ctx->stream));
+    s->p_null = h[1] > 0.0 && h[0] <= 1e-10 * h[1];
+    s->p_null_gen = ctx->params_gen;
+  }
+  if (!s->p_null) return 0;
+  S_CUDA(cudaMemsetAsync(s->gsum, 0, sizeof(double), ctx->stream));
+  { k_range_sum<<<grid_for(ctx, pe - pb), 256, 0, ctx->stream>>>(delta, pb, pe, s->gsum); gbmhd::count_launch(); }
+  { k_range_shift<<<grid_for(ctx, pe - pb), 256, 0, ctx->stream>>>(delta, pb, pe, s->gsum); gbmhd::count_launch(); }
+  S_CUDA(cudaGetLastError());
+  return 0;
+}
+
 static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
   auto t0 = std::chrono::steady_clock::now();
   Solver* s = ctx->solver;
@@ -677,7 +754,7 @@ void solver_destroy(gbmhd_ctx* ctx) {
   if (!s) return;
   mf_destroy(s->mf);
   void* ptrs[] = {s->reg, s->Mp_inv, s->Mf_inv, s->seg, s->V, s->Z, s->w, s->t1, s->t2, s->x32, s->part,
-                  s->hdev, s->permT, s->valT};
+                  s->hdev, s->permT, s->valT, s->gsum};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->hhost) cudaFreeHost(s->hhost);
@@ -811,6 +888,7 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     }
     // a preconditioner application whose TMA copies timed out was cut short: fail this step
     if (ctx->solver->mf && (rc = mf_check_sweeps(ctx, ctx->solver->mf))) return rc;
+    if ((rc = project_pressure_gauge(ctx, r))) return rc;
     { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, r, 1.0, d_x); gbmhd::count_launch(); }
     S_CUDA(cudaStreamSynchronize(ctx->stream));
     R.time_linear_s += now_s() - tl;

@@ -23,7 +23,7 @@ GBMHD_PC_BADIA2024 = 1
 
 SYMBOLS = ["gbmhd_version", "gbmhd_create", "gbmhd_set_params", "gbmhd_sizes", "gbmhd_assemble",
            "gbmhd_assemble_device", "gbmhd_get_csr", "gbmhd_newton_solve", "gbmhd_newton_solve_device",
-           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_sweep_stats", "gbmhd_hunt_errors", "gbmhd_diag_tc_gemm", "gbmhd_diag_pc_compare", "gbmhd_node_fields", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
+           "gbmhd_adjoint", "gbmhd_param_gradient_noalloc", "gbmhd_get_stream", "gbmhd_diag_uj_solve_error", "gbmhd_sweep_stats", "gbmhd_hunt_errors", "gbmhd_diag_tc_gemm", "gbmhd_diag_pivot_inverse", "gbmhd_diag_pc_compare", "gbmhd_node_fields", "gbmhd_counters", "gbmhd_last_error", "gbmhd_destroy"]
 
 _dp = C.POINTER(C.c_double)
 _i32p = C.POINTER(C.c_int32)
@@ -121,6 +121,8 @@ def load(path: Optional[str] = None):
                                       C.c_void_p, C.c_int32, C.c_int64, C.c_float, C.c_void_p, C.c_int32,
                                       C.c_int64, C.c_int32, C.POINTER(C.c_int32)]
     L.gbmhd_diag_pc_compare.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, _dp]
+    L.gbmhd_diag_pivot_inverse.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                            C.c_int32, _dp, C.POINTER(C.c_int32)]
     L.gbmhd_node_fields.argtypes = [C.c_void_p, _dp, _dp]
     L.gbmhd_hunt_errors.argtypes = [C.c_void_p, _dp, C.POINTER(HuntAnalytic), _dp]
     L.gbmhd_counters.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]

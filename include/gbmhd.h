@@ -250,9 +250,16 @@ int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double*
  *                                   that has run GBMHD_STAG_ITERS iterations (default 100) with
  *                                   its relative residual still above GBMHD_STAG_REL (default
  *                                   0.5) triggers the refactorization / FP64 fallback
+ *   GBMHD_PIVOT_KERNEL              force one pivot-block inverse kernel of the FP32 factors
+ *                                   (the variants of gbmhd_diag_pivot_inverse; read per factorization)
+ *   GBMHD_MF_LEVEL_TIMES            print each factorization's per-level device time (CUDA
+ *                                   events) and host issue time to stderr
  *   GBMHD_SWEEP_GRAPHS              0: launch the kernels of each preconditioner application one
  *                                   by one instead of replaying them as a CUDA graph (for per-kernel
  *                                   profiling; read when a context first factors; default 1)
+ *   GBMHD_SWEEP_BRANCHES            0: substitute the level groups of one tree height one after
+ *                                   another instead of side by side on branch streams (read when a
+ *                                   context first factors; default 1)
  *   GBMHD_SWEEP_WAIT_LIMIT          spin limit of the TMA solve sweeps' mbarrier waits, read
  *                                   when a context first factors (default 4,194,304); a wait
  *                                   that runs out drains its copies and makes the Newton step
@@ -262,6 +269,18 @@ int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double*
  * (transpose = 1) for a seeded random b, with the monolithic preconditioner factored in FP32
  * (from the FP32 Jacobian) and in FP64, both assembled at the device state d_state. */
 int gbmhd_diag_pc_compare(gbmhd_ctx* ctx, const double* d_state, int32_t transpose, double* err);
+
+/* Diagnostic: the float-float Gauss-Jordan inverse of the FP32 factorization's NB x NB
+ * (64 x 64) diagonal pivot blocks, with partial pivoting inside the block: for each of `count`
+ * column-major n x n fronts in the device buffer F, the leading kb x kb block's inverse goes
+ * to P (count blocks of 64 x 64, column-major, zero outside kb x kb).  variant selects the
+ * kernel (0: 16 column groups of 64 rows, 1: 4 column groups, 2: block in shared memory,
+ * 3: one column pair per warp, one barrier per column step); all give the same bits.  After
+ * one checked launch, `reps` more are timed with CUDA events (*ms_per_launch).  Synchronises
+ * the device; *status = 1 if a block was singular.  No counterpart in the reference (its
+ * dense kernels are UMFPACK's, src/main.jl:181-186). */
+int gbmhd_diag_pivot_inverse(int32_t variant, int32_t count, int32_t n, int32_t kb, const float* F, float* P,
+                             int32_t reps, double* ms_per_launch, int32_t* status);
 
 /* Diagnostic: the FP32 strided-batched GEMM of the factorization's dense updates, on the
  * tcgen05 tensor cores (three-way BF16 splits of each operand, six cross products, FP32
