@@ -92,6 +92,9 @@ struct MFNumeric {
   std::vector<cudaStream_t> bstreams;
   std::vector<cudaEvent_t> fev;
   std::vector<int32_t> lheight;
+  // per factorization lane beyond the first: pivot-block, block-column and GEMM scratch
+  std::vector<void*> lane_buf;
+  std::vector<size_t> lane_bytes;
   bool ev_pending = false;
   int64_t sweep_applies = 0;
   double sweep_seconds = 0.0;
@@ -264,6 +267,8 @@ void mf_destroy(MFNumeric* M) {
     if (e) cudaEventDestroy(e);
   for (cudaStream_t st : M->bstreams)
     if (st) cudaStreamDestroy(st);
+  for (void* p : M->lane_buf)
+    if (p) cudaFree(p);
   if (M->s2) cudaStreamDestroy(M->s2);
   delete M;
 }
@@ -668,15 +673,15 @@ __global__ void __launch_bounds__(NB * CGN) k_pivot_inverse_df(const float* __re
 // float-float reciprocal of the pivot and the multipliers m_i = A[i, c + 1] after the
 // interchange; after the step's one barrier every warp forms its own entries of the scaled
 // pivot row with warp shuffles.  Every entry goes through the same operations, in the same
-// order, as in k_pivot_inverse_df, so the two kernels give the same bits.
-__global__ void __launch_bounds__(1024) k_pivot_inverse_dfw(const float* __restrict__ F, int64_t off, int n, int k,
+// order, as in k_pivot_inverse_df, so the two kernels give the same bits.  Shared memory:
+// ~2 KB (the multipliers and the interchanges), so the CTA fits on an SM beside a
+// tensor-core GEMM CTA.
+__global__ void __maxnreg__(40) k_pivot_inverse_dfw(const float* __restrict__ F, int64_t off, int n, int k,
                                                            int kb, float* __restrict__ P, int32_t* err) {
-  constexpr int LD = NB + 1;
-  __shared__ float Ob[NB * LD];
   __shared__ float mh[2][NB], ml[2][NB];
   __shared__ float sih[2], sil[2];
   __shared__ int spr[2];
-  __shared__ int perm[NB], colsrc[NB];
+  __shared__ int perm[NB], colsrc[NB], cdst[NB];
   const int64_t f = blockIdx.x;
   const float* M = F + off + f * (int64_t)n * n;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -774,24 +779,30 @@ __global__ void __launch_bounds__(1024) k_pivot_inverse_dfw(const float* __restr
     if (c + 1 < kb && w == ((c + 1) & 31)) publish(c + 1);
     __syncthreads();
   }
-#pragma unroll
-  for (int s = 0; s < 2; ++s)
-#pragma unroll
-    for (int q = 0; q < 2; ++q) Ob[(lane + 32 * q) + (w + 32 * s) * LD] = __fadd_rn(h[s][q], l[s][q]);
   if (threadIdx.x == 0) {  // undo the row interchanges as column interchanges, last first
-    for (int j = 0; j < kb; ++j) colsrc[j] = j;
+    for (int j = 0; j < NB; ++j) colsrc[j] = j;
     for (int c = kb - 1; c >= 0; --c) {
       const int p = perm[c];
       const int t = colsrc[c];
       colsrc[c] = colsrc[p];
       colsrc[p] = t;
     }
+    for (int j = 0; j < NB; ++j) cdst[colsrc[j]] = j;
   }
   __syncthreads();
+  // each warp stores its two columns where the interchanges put them (column-major, zero
+  // outside kb x kb); the block needs no staging buffer, so its CTA fits beside a
+  // tensor-core GEMM CTA on one SM
   float* Pf = P + f * (int64_t)NB * NB;
-  const int ti = threadIdx.x & (NB - 1), tj = threadIdx.x >> 6;
-  for (int j = tj; j < NB; j += 16)  // column-major, zero outside kb x kb
-    Pf[ti + j * NB] = (ti < kb && j < kb) ? Ob[ti + colsrc[j] * LD] : 0.0f;
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    const int cs = w + 32 * s, j = cdst[cs];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int i = lane + 32 * q;
+      Pf[i + j * NB] = (i < kb && cs < kb) ? __fadd_rn(h[s][q], l[s][q]) : 0.0f;
+    }
+  }
 }
 
 // Shared-memory variant (block in shared memory, 6 CTAs per SM): levels with many fronts,
@@ -2317,14 +2328,25 @@ static int tma_cols(const gbmhd_ctx* ctx, int64_t rows, int tile_rows, int64_t n
 // C = α·A·B + β·C for the fronts of a level (strided-batched, column-major).  FP32 factors use
 // the library's tensor-core GEMM (tc_gemm.cu); FP64 factors (the plain FP64 path) use cuBLAS
 // DGEMM.
+// One factorization lane: a stream and the scratch of the levels it factors.
 template <typename T>
-static int gemm(gbmhd_ctx* ctx, MFNumeric* M, int m, int n, int k, T alpha, const T* A, int lda, long long sA,
-                const T* B, int ldb, long long sB, T beta, T* C, int ldc, long long sC, int batch) {
+struct FactorLane {
+  cudaStream_t st = nullptr;
+  T* P = nullptr;        // diagonal-block inverses  [count][NB*NB]
+  T* C = nullptr;        // column block below a pivot block [count][n*NB]
+  void* gws = nullptr;   // split images of the FP32 GEMM operands
+  size_t gws_bytes = 0;
+};
+
+template <typename T>
+static int gemm(gbmhd_ctx* ctx, MFNumeric* M, const FactorLane<T>& lane, int m, int n, int k, T alpha, const T* A,
+                int lda, long long sA, const T* B, int ldb, long long sB, T beta, T* C, int ldc, long long sC,
+                int batch) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
   if constexpr (sizeof(T) == 4) {
     std::string msg;
-    const int rc = gbmhd::tc_gemm_f32(ctx->stream, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch,
-                                      M->gws, M->gws_bytes, M->d_err, &msg);
+    const int rc = gbmhd::tc_gemm_f32(lane.st, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch,
+                                      lane.gws, lane.gws_bytes, M->d_err, &msg);
     if (rc) ctx->err = "multifrontal: " + msg;
     return rc;
   } else {
@@ -2399,8 +2421,6 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
     }
   }
   T* F = reinterpret_cast<T*>(M->F);
-  T* P = reinterpret_cast<T*>(M->Pbuf);
-  T* C = reinterpret_cast<T*>(M->Cbuf);
   MF_CUDA(cudaMemsetAsync(M->d_err, 0, sizeof(int32_t), ctx->stream));
   // level sizes on the device for the extend-add kernel
   std::vector<int> ln(S.levels.size()), le(S.levels.size());
@@ -2414,7 +2434,7 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
   const char* pks = std::getenv("GBMHD_PIVOT_KERNEL");
   const int pk = pks ? std::atoi(pks) : -1;
   // GBMHD_MF_LEVEL_TIMES: device time of each level (CUDA events) and the host's time to
-  // issue it, printed to stderr
+  // issue it, printed to stderr (the levels then run one after another)
   const bool ltimes = std::getenv("GBMHD_MF_LEVEL_TIMES") != nullptr;
   std::vector<cudaEvent_t> lev_ev;
   std::vector<double> lev_host;
@@ -2423,27 +2443,92 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
     for (cudaEvent_t& e : lev_ev) MF_CUDA(cudaEventCreate(&e));
     lev_host.resize(S.levels.size() + 1);
   }
-  for (size_t l = 0; l < S.levels.size(); ++l) {
+  // Lanes: the level groups of one tree height are independent (each assembles, extend-adds
+  // and eliminates its own fronts; their children are lower), so with FP32 factors they run
+  // side by side, the first group on the context stream and the others on the branch
+  // streams, each lane with its own pivot-block, block-column and GEMM scratch.
+  const size_t nlev = S.levels.size();
+  std::vector<int> lane_of(nlev, 0);
+  int nlanes = 1;
+  if (sizeof(T) == 4 && !ltimes && !M->bstreams.empty()) {
+    nlanes = 1 + (int)M->bstreams.size();
+    for (size_t la = 0; la < nlev;) {
+      size_t lb = la + 1;
+      while (lb < nlev && M->lheight[lb] == M->lheight[la]) ++lb;
+      for (size_t i = 1; i < lb - la; ++i) lane_of[la + i] = 1 + (int)((i - 1) % (nlanes - 1));
+      la = lb;
+    }
+  }
+  auto level_scratch = [&](const MFLevel& L, size_t* pb, size_t* cb, size_t* gb) {
+    const int pw = std::min(PW, L.E), kb = std::min(NB, L.E), cnt = (int)L.count;
+    *pb = sizeof(T) * (size_t)L.count * NB * NB;
+    *cb = sizeof(T) * (size_t)L.count * L.n * NB;
+    *gb = 0;
+    if (sizeof(T) == 4) {
+      *gb = std::max(*gb, gbmhd::tc_gemm_workspace(L.n - kb, kb, kb, cnt));
+      *gb = std::max(*gb, gbmhd::tc_gemm_workspace(kb, L.n - pw, pw, cnt));
+      *gb = std::max(*gb, gbmhd::tc_gemm_workspace(L.n - pw, L.n - pw, pw, cnt));
+    }
+  };
+  if (nlanes > 1) {
+    std::vector<size_t> need(3 * nlanes, 0);
+    for (size_t l = 0; l < nlev; ++l) {
+      if (!lane_of[l]) continue;
+      size_t pb, cb, gb;
+      level_scratch(S.levels[l], &pb, &cb, &gb);
+      const int i = lane_of[l];
+      need[3 * i] = std::max(need[3 * i], pb);
+      need[3 * i + 1] = std::max(need[3 * i + 1], cb);
+      need[3 * i + 2] = std::max(need[3 * i + 2], gb);
+    }
+    size_t more = 0;
+    for (int i = 1; i < nlanes; ++i)
+      for (int q = 0; q < 3; ++q)
+        if (M->lane_bytes.size() <= (size_t)(3 * i + q) || M->lane_bytes[3 * i + q] < need[3 * i + q]) more += need[3 * i + q];
+    size_t free_b = 0, total_b = 0;
+    MF_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (more + ((size_t)2 << 30) > free_b) {
+      nlanes = 1;  // not worth the memory: the levels run in sequence
+      std::fill(lane_of.begin(), lane_of.end(), 0);
+    } else {
+      M->lane_buf.resize(3 * nlanes, nullptr);
+      M->lane_bytes.resize(3 * nlanes, 0);
+      for (int i = 1; i < nlanes; ++i)
+        for (int q = 0; q < 3; ++q) {
+          const int j = 3 * i + q;
+          if (M->lane_bytes[j] >= need[j]) continue;
+          if (M->lane_buf[j]) cudaFree(M->lane_buf[j]);
+          M->lane_buf[j] = nullptr;
+          M->lane_bytes[j] = 0;
+          MF_CUDA(cudaMalloc(&M->lane_buf[j], std::max<size_t>(need[j], 16)));
+          M->lane_bytes[j] = std::max<size_t>(need[j], 16);
+        }
+    }
+  }
+  std::vector<FactorLane<T>> lanes(nlanes);
+  lanes[0] = FactorLane<T>{ctx->stream, reinterpret_cast<T*>(M->Pbuf), reinterpret_cast<T*>(M->Cbuf), M->gws,
+                           M->gws_bytes};
+  for (int i = 1; i < nlanes; ++i)
+    lanes[i] = FactorLane<T>{M->bstreams[i - 1], reinterpret_cast<T*>(M->lane_buf[3 * i]),
+                             reinterpret_cast<T*>(M->lane_buf[3 * i + 1]), M->lane_buf[3 * i + 2],
+                             M->lane_bytes[3 * i + 2]};
+  auto factor_level = [&](size_t l, const FactorLane<T>& lane) -> int {
     const MFLevel& L = S.levels[l];
     const int n = L.n, E = L.E;
-    if (ltimes) {
-      MF_CUDA(cudaEventRecord(lev_ev[l], ctx->stream));
-      lev_host[l] = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
-    }
     const int cnt = (int)L.count;
     const long long sn = (long long)n * n;  // front stride
     T* F0 = F + L.off;
-    MF_CUDA(cudaMemsetAsync(F0, 0, sizeof(T) * (size_t)L.count * n * n, ctx->stream));
-    { k_pad_diag<T><<<cnt, 128, 0, ctx->stream>>>(F, L.off, L.count, n, E, M->d.f_ne, L.first); gbmhd::count_launch(); }
+    MF_CUDA(cudaMemsetAsync(F0, 0, sizeof(T) * (size_t)L.count * n * n, lane.st));
+    { k_pad_diag<T><<<cnt, 128, 0, lane.st>>>(F, L.off, L.count, n, E, M->d.f_ne, L.first); gbmhd::count_launch(); }
     const int64_t nah = L.ah_end - L.ah_begin;
     if (nah > 0) {
       int64_t g = std::min<int64_t>((nah + 255) / 256, (int64_t)ctx->num_sms * 16);
-      { k_arrowhead<T, V><<<(unsigned)g, 256, 0, ctx->stream>>>(Aval, M->d.ah_src, M->d.ah_dst, L.ah_begin, L.ah_end, F); gbmhd::count_launch(); }
+      { k_arrowhead<T, V><<<(unsigned)g, 256, 0, lane.st>>>(Aval, M->d.ah_src, M->d.ah_dst, L.ah_begin, L.ah_end, F); gbmhd::count_launch(); }
     }
     if (l + 1 == S.levels.size() && d_reg && !S.reg_dst.empty()) {
       // the global p and φ representatives are eliminated in the root front
       const int64_t nr = (int64_t)S.reg_dst.size();
-      { k_reg_add<T><<<(unsigned)std::min<int64_t>((nr + 255) / 256, 4096), 256, 0, ctx->stream>>>(F, M->d.reg_dst, M->d.reg_dof, d_reg, M->scaled ? M->d_dr : nullptr, M->d_dc, nr); gbmhd::count_launch(); }
+      { k_reg_add<T><<<(unsigned)std::min<int64_t>((nr + 255) / 256, 4096), 256, 0, lane.st>>>(F, M->d.reg_dst, M->d.reg_dof, d_reg, M->scaled ? M->d_dr : nullptr, M->d_dc, nr); gbmhd::count_launch(); }
     }
     const int64_t nch = L.ch_end - L.ch_begin;
     if (nch > 0) {
@@ -2451,7 +2536,7 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
       for (int64_t c = L.ch_begin; c < L.ch_end; ++c) maxb = std::max(maxb, S.f_nb[S.child_list[c]]);
       const int gy = std::max(1, std::min(maxb, std::max(1, (int)(ctx->num_sms * 32 / nch))));
       dim3 grid((unsigned)nch, (unsigned)gy);
-      { k_extend_add<T><<<grid, 256, 0, ctx->stream>>>(F, M->d.child_list, L.ch_begin, M->d.f_nb, M->d.f_off,
+      { k_extend_add<T><<<grid, 256, 0, lane.st>>>(F, M->d.child_list, L.ch_begin, M->d.f_nb, M->d.f_off,
                                                      M->d.f_parent, M->d.f_level, M->d.ea_ptr, M->d.ea_pos, d_ln, d_le); gbmhd::count_launch(); }
     }
     MF_CUDA(cudaGetLastError());
@@ -2466,15 +2551,15 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
         const int kb = std::min(NB, p + pw - k);
         if constexpr (sizeof(T) == 4)
           {
-            launch_pivot_inverse(pivot_variant(ctx, cnt, pk), cnt, ctx->stream, F, L.off, n, k, kb, P, M->d_err);
+            launch_pivot_inverse(pivot_variant(ctx, cnt, pk), cnt, lane.st, F, L.off, n, k, kb, lane.P, M->d_err);
             gbmhd::count_launch();
           }
         else
-          { k_pivot_inverse<T><<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P, M->d_err); gbmhd::count_launch(); }
+          { k_pivot_inverse<T><<<cnt, 256, 0, lane.st>>>(F, L.off, n, k, kb, lane.P, M->d_err); gbmhd::count_launch(); }
         const int rb = n - (k + kb);  // rows below the block (eliminated and boundary)
         if (rb > 0) {
           dim3 gc((unsigned)kb, (unsigned)cnt);
-          { k_copy_block<T><<<gc, 256, 0, ctx->stream>>>(F, L.off, n, k + kb, rb, k, kb, C); gbmhd::count_launch(); }
+          { k_copy_block<T><<<gc, 256, 0, lane.st>>>(F, L.off, n, k + kb, rb, k, kb, lane.C); gbmhd::count_launch(); }
           MF_CUDA(cudaGetLastError());
           T* Lk = F0 + (k + kb) + (int64_t)k * n;  // M[below, K]
           const T* Dk = F0 + k + (int64_t)k * n;   // M[K, K], still the block itself
@@ -2484,17 +2569,17 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
           // L = L₀ + R·D⁻¹.  The FP32 inverse carries errors of κ(D)·2⁻²⁴; without the step they
           // enter the Schur complements (FP32 emulation, 24x24x4 at Ha = 500: 15 → 5 FGMRES
           // iterations to 1e-10 on the first Newton system).
-          if ((rc = gemm<T>(ctx, M, rb, kb, kb, one, C, n, sC, P, NB, sP, zero, Lk, n, sn, cnt))) return rc;
+          if ((rc = gemm<T>(ctx, M, lane, rb, kb, kb, one, lane.C, n, sC, lane.P, NB, sP, zero, Lk, n, sn, cnt))) return rc;
           if constexpr (sizeof(T) == 4) {
-            if ((rc = gemm<T>(ctx, M, rb, kb, kb, mone, Lk, n, sn, Dk, n, sn, one, C, n, sC, cnt))) return rc;
-            if ((rc = gemm<T>(ctx, M, rb, kb, kb, one, C, n, sC, P, NB, sP, one, Lk, n, sn, cnt))) return rc;
+            if ((rc = gemm<T>(ctx, M, lane, rb, kb, kb, mone, Lk, n, sn, Dk, n, sn, one, lane.C, n, sC, cnt))) return rc;
+            if ((rc = gemm<T>(ctx, M, lane, rb, kb, kb, one, lane.C, n, sC, lane.P, NB, sP, one, Lk, n, sn, cnt))) return rc;
           }
           const int cr = p + pw - (k + kb);  // the panel's later columns
-          if (cr > 0 && (rc = gemm<T>(ctx, M, rb, cr, kb, mone, Lk, n, sn, F0 + k + (int64_t)(k + kb) * n, n, sn,
+          if (cr > 0 && (rc = gemm<T>(ctx, M, lane, rb, cr, kb, mone, Lk, n, sn, F0 + k + (int64_t)(k + kb) * n, n, sn,
                                       one, F0 + (k + kb) + (int64_t)(k + kb) * n, n, sn, cnt)))
             return rc;
         }
-        { k_put_inverse<T><<<cnt, 256, 0, ctx->stream>>>(F, L.off, n, k, kb, P); gbmhd::count_launch(); }
+        { k_put_inverse<T><<<cnt, 256, 0, lane.st>>>(F, L.off, n, k, kb, lane.P); gbmhd::count_launch(); }
         MF_CUDA(cudaGetLastError());
       }
       const int c0 = p + pw, rest = n - c0;
@@ -2502,16 +2587,44 @@ static int factor_impl(gbmhd_ctx* ctx, MFNumeric* M, const V* Aval, const double
         int rc = 0;
         for (int k = p + NB; k < p + pw; k += NB) {  // U rows of the panel's later blocks
           const int kb = std::min(NB, p + pw - k);
-          if ((rc = gemm<T>(ctx, M, kb, rest, k - p, mone, F0 + k + (int64_t)p * n, n, sn, F0 + p + (int64_t)c0 * n, n,
+          if ((rc = gemm<T>(ctx, M, lane, kb, rest, k - p, mone, F0 + k + (int64_t)p * n, n, sn, F0 + p + (int64_t)c0 * n, n,
                             sn, one, F0 + k + (int64_t)c0 * n, n, sn, cnt)))
             return rc;
         }
         // trailing update: M[c0:, c0:] −= M[c0:, panel] · M[panel, c0:]
-        if ((rc = gemm<T>(ctx, M, rest, rest, pw, mone, F0 + c0 + (int64_t)p * n, n, sn, F0 + p + (int64_t)c0 * n, n,
+        if ((rc = gemm<T>(ctx, M, lane, rest, rest, pw, mone, F0 + c0 + (int64_t)p * n, n, sn, F0 + p + (int64_t)c0 * n, n,
                           sn, one, F0 + c0 + (int64_t)c0 * n, n, sn, cnt)))
           return rc;
       }
     }
+    return 0;
+  };
+  size_t fvn = 0;
+  auto next_fev = [&]() { return M->fev[fvn++ % M->fev.size()]; };
+  for (size_t la = 0; la < nlev;) {
+    size_t lb = la + 1;
+    while (lb < nlev && M->lheight[lb] == M->lheight[la]) ++lb;
+    int used = 0;
+    for (size_t l = la; l < lb; ++l) used = std::max(used, lane_of[l]);
+    if (used > 0) {
+      cudaEvent_t fork = next_fev();
+      MF_CUDA(cudaEventRecord(fork, ctx->stream));
+      for (int i = 1; i <= used; ++i) MF_CUDA(cudaStreamWaitEvent(lanes[i].st, fork, 0));
+    }
+    for (size_t l = la; l < lb; ++l) {
+      if (ltimes) {
+        MF_CUDA(cudaEventRecord(lev_ev[l], ctx->stream));
+        lev_host[l] = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+      }
+      int rc = factor_level(l, lanes[lane_of[l]]);
+      if (rc) return rc;
+    }
+    for (int i = 1; i <= used; ++i) {
+      cudaEvent_t join = next_fev();
+      MF_CUDA(cudaEventRecord(join, lanes[i].st));
+      MF_CUDA(cudaStreamWaitEvent(ctx->stream, join, 0));
+    }
+    la = lb;
   }
   if (ltimes) {
     MF_CUDA(cudaEventRecord(lev_ev.back(), ctx->stream));

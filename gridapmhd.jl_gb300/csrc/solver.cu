@@ -473,18 +473,24 @@ static int ensure_workspace(gbmhd_ctx* ctx, int m) {
 constexpr double kEps32 = 1e-3;
 
 // Preconditioner set-up: (u,j) factorization + mass blocks.
-// Removes the constant-pressure component from a Newton update δ (δ_p −= mean δ_p) when the
-// all-ones vector on the p dofs is a null vector of the Jacobian: the pressure is then defined
-// up to a constant, and the preconditioner (whose root carries −ε·mass on the global p
-// representatives) amplifies that component of the residual's rounding by ~1/ε.  Left in
-// place, it lets the pressure level drift from step to step, and the rounding of the FP64
-// residual grows with it until Newton stalls above its tolerance.  J·1_p = 0, so the removal
-// changes no J·δ.  The null test uses the FP64 Jacobian (assembled before each Newton step):
+// Removes the constant-pressure component from a preconditioned FGMRES direction z (z_p −= mean
+// z_p) when the all-ones vector on the p dofs is a null vector of the Jacobian (velocity fixed
+// on every wall; then also of its transpose).  The pressure is then defined up to a constant
+// that the Krylov relation cannot see, and the preconditioner (whose root carries −ε·mass on
+// the global p representatives) puts a large, arbitrary amount of that mode into every z.
+// Summed into the update, it lets the pressure level drift by O(100) per Newton step, and the
+// FP64 residual's rounding, which grows with |p|, stalls Newton above its tolerance.  Removing
+// it from each z before J·z is formed keeps the Arnoldi relation exact for the vectors the
+// update is built from (removing it from the update afterwards would not: J·1_p vanishes only
+// to rounding, and times an O(100) constant that is already the size of the last steps'
+// residuals).  The null test uses the FP64 Jacobian:
 // max_r |Σ_p J[r, p]| ≤ 1e-10 · max_r Σ_p |J[r, p]|.
-static int project_pressure_gauge(gbmhd_ctx* ctx, double* delta) {
+static int project_pressure_gauge(gbmhd_ctx* ctx, double* z) {
   Solver* s = ctx->solver;
   const int64_t pb = ctx->offs[1], pe = ctx->offs[2];
   if (pe <= pb || !ctx->d_val64) return 0;
+  if (const char* g = std::getenv("GBMHD_GAUGE_PROJECTION"))
+    if (std::atoi(g) == 0) return 0;
   if (!s->gsum) S_CUDA(cudaMalloc(&s->gsum, 2 * sizeof(double)));
   if (s->p_null < 0 || s->p_null_gen != ctx->params_gen) {
     S_CUDA(cudaMemsetAsync(s->gsum, 0, 2 * sizeof(double), ctx->stream));
@@ -497,8 +503,8 @@ static int project_pressure_gauge(gbmhd_ctx* ctx, double* delta) {
   }
   if (!s->p_null) return 0;
   S_CUDA(cudaMemsetAsync(s->gsum, 0, sizeof(double), ctx->stream));
-  { k_range_sum<<<grid_for(ctx, pe - pb), 256, 0, ctx->stream>>>(delta, pb, pe, s->gsum); gbmhd::count_launch(); }
-  { k_range_shift<<<grid_for(ctx, pe - pb), 256, 0, ctx->stream>>>(delta, pb, pe, s->gsum); gbmhd::count_launch(); }
+  { k_range_sum<<<grid_for(ctx, pe - pb), 256, 0, ctx->stream>>>(z, pb, pe, s->gsum); gbmhd::count_launch(); }
+  { k_range_shift<<<grid_for(ctx, pe - pb), 256, 0, ctx->stream>>>(z, pb, pe, s->gsum); gbmhd::count_launch(); }
   S_CUDA(cudaGetLastError());
   return 0;
 }
@@ -691,6 +697,7 @@ static int fgmres(gbmhd_ctx* ctx, int precision, const double* b, double* x, int
       double* vk = s->V + (int64_t)k * n;
       double* zk = s->Z + (int64_t)k * n;
       if ((rc = apply_pc(ctx, precision, vk, zk, transpose))) return rc;
+      if ((rc = project_pressure_gauge(ctx, zk))) return rc;
       if ((rc = op(zk, s->w))) return rc;
       // CGS2 with the coefficients kept on the device; one host round trip per iteration
       if ((rc = dot_dev(ctx, s, s->V, k + 1, s->w, s->hdev))) return rc;
@@ -888,7 +895,6 @@ extern "C" int gbmhd_newton_solve_device(gbmhd_ctx* ctx, double* d_x, const gbmh
     }
     // a preconditioner application whose TMA copies timed out was cut short: fail this step
     if (ctx->solver->mf && (rc = mf_check_sweeps(ctx, ctx->solver->mf))) return rc;
-    if ((rc = project_pressure_gauge(ctx, r))) return rc;
     { k_axpby<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(n, 1.0, r, 1.0, d_x); gbmhd::count_launch(); }
     S_CUDA(cudaStreamSynchronize(ctx->stream));
     R.time_linear_s += now_s() - tl;

@@ -254,6 +254,7 @@ int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double*
  *                                   (the variants of gbmhd_diag_pivot_inverse; read per factorization)
  *   GBMHD_MF_LEVEL_TIMES            print each factorization's per-level device time (CUDA
  *                                   events) and host issue time to stderr
+ *   GBMHD_GAUGE_PROJECTION          0: keep the constant-pressure component of the Newton updates
  *   GBMHD_SWEEP_GRAPHS              0: launch the kernels of each preconditioner application one
  *                                   by one instead of replaying them as a CUDA graph (for per-kernel
  *                                   profiling; read when a context first factors; default 1)

@@ -108,9 +108,10 @@ def test_cfg4_48x48x4_adjoint_gradient(gpu_lib):
 
     # (2) central finite differences of FP64 GPU Newton solves from x.  The J of a solve carries
     # the FP64 residual floor (1e-12 … 5e-11 absolute, the assembly's atomic adds in arbitrary
-    # order): measured 3e-14 … 1.4e-13 in J, i.e. up to ~5e-6 of the gradient at a relative
-    # step of 1e-6.  So the 1e-6 step is checked to 1e-5, and a 1e-4 step (truncation
-    # O(h²) ~ 1e-8, noise 100x smaller) to the 1e-6 target.
+    # order): measured 3e-14 … 1.4e-13 in J, i.e. mostly 1e-8 … 5e-6 of the gradient at a
+    # relative step of 1e-6, with one cw difference at 2.5e-5 in four runs.  So the 1e-6 step is
+    # checked to 5e-5, and a 1e-4 step (truncation O(h²) ~ 1e-8, noise 100x smaller) to the
+    # 1e-6 target.
     fd_opts = dict(max_newton=6, newton_rtol=0.0, newton_atol=0.0, linear_rtol=1e-12, **base)
 
     def J(p):
@@ -121,7 +122,7 @@ def test_cfg4_48x48x4_adjoint_gradient(gpu_lib):
     f = params["facets"]
     w = np.random.default_rng(1).uniform(0.5, 1.5, mesh.ncells) * params["f_cell"][:, 2]
     adj = {"Ha": dJ_dHa, "cw": dJ[1], "f_z": float(dJ[4:] @ w)}
-    for h, tol in ((1e-6, 1e-5), (1e-4, 1e-6)):
+    for h, tol in ((1e-6, 5e-5), (1e-4, 1e-6)):
         fd = {}
         pp = dict(params, gamma=(Ha * (1 + h)) ** 2 / Re)
         pm = dict(params, gamma=(Ha * (1 - h)) ** 2 / Re)
