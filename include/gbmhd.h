@@ -253,14 +253,16 @@ int gbmhd_sweep_stats(gbmhd_ctx* ctx, int64_t* applies, double* seconds, double*
  *   GBMHD_PIVOT_KERNEL              force one pivot-block inverse kernel of the FP32 factors
  *                                   (the variants of gbmhd_diag_pivot_inverse; read per factorization)
  *   GBMHD_MF_LEVEL_TIMES            print each factorization's per-level device time (CUDA
- *                                   events) and host issue time to stderr
- *   GBMHD_GAUGE_PROJECTION          0: keep the constant-pressure component of the Newton updates
+ *                                   events) and host issue time to stderr (levels in sequence)
+ *   GBMHD_GAUGE_PROJECTION          0: keep the constant-pressure component of the FGMRES
+ *                                   directions (removed by default when the all-ones p vector is
+ *                                   a null vector of the Jacobian)
  *   GBMHD_SWEEP_GRAPHS              0: launch the kernels of each preconditioner application one
  *                                   by one instead of replaying them as a CUDA graph (for per-kernel
  *                                   profiling; read when a context first factors; default 1)
- *   GBMHD_SWEEP_BRANCHES            0: substitute the level groups of one tree height one after
- *                                   another instead of side by side on branch streams (read when a
- *                                   context first factors; default 1)
+ *   GBMHD_SWEEP_BRANCHES            0: substitute and factor the level groups of one tree height
+ *                                   one after another instead of side by side on branch streams
+ *                                   (read when a context first factors; default 1)
  *   GBMHD_SWEEP_WAIT_LIMIT          spin limit of the TMA solve sweeps' mbarrier waits, read
  *                                   when a context first factors (default 4,194,304); a wait
  *                                   that runs out drains its copies and makes the Newton step
