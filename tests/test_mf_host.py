@@ -98,3 +98,50 @@ def test_levels_keep_eliminated_and_boundary_dofs_apart(harness, mono, case):
         for f in range(first, first + count):
             b = S["bnd"][S["bnd_ptr"][f]:S["bnd_ptr"][f + 1]]
             assert len(np.unique(b)) == len(b)
+
+
+@pytest.mark.parametrize("mono", [True, False])
+@pytest.mark.parametrize("case", [dict(nc=(8, 8), nz=3, Ha=10.0, Re=10.0, cw=0.01, Lz=0.2),
+                                  dict(nc=(16, 16), nz=4, Ha=500.0, Re=1.0, beta_map=3.0, cw=0.1, Lz=0.2)])
+def test_groups_of_one_height_are_independent(harness, mono, case):
+    """The sweeps and the FP32 factorization run the level groups of one tree height side by
+    side (csrc/mf_numeric.cu: lheight from f_parent, one run per height).  That needs: a
+    parent follows its children in the front order (the heights are computed in one pass);
+    the fronts of a group share one height and a height's groups are consecutive; no front's
+    parent lies in a group of its own height; and every boundary dof of a front is
+    eliminated by one of its ancestors, so groups of one height write disjoint eliminated
+    dofs and only add (atomically) into higher fronts' dofs."""
+    mesh, dm, params = hunt_case(**case)
+    S = symbolic(harness, mesh, dm, mono)
+    fp = S["f_parent"]
+    nf = len(fp)
+    fh = np.zeros(nf, np.int64)
+    for f in range(nf):
+        if fp[f] >= 0:
+            assert fp[f] > f
+            fh[fp[f]] = max(fh[fp[f]], fh[f] + 1)
+    lev_h = []
+    lev_of = np.zeros(nf, np.int64)
+    for l, L in enumerate(S["levels"]):
+        first, count = int(L[3]), int(L[4])
+        assert count > 0
+        assert len(set(fh[first:first + count].tolist())) == 1
+        lev_h.append(int(fh[first]))
+        lev_of[first:first + count] = l
+    assert lev_h == sorted(lev_h)  # each height's groups are consecutive
+    for f in range(nf):
+        if fp[f] >= 0:
+            assert lev_h[lev_of[fp[f]]] > lev_h[lev_of[f]]
+    owner = np.full(dm.ndofs, -1, np.int64)
+    for f in range(nf):
+        owner[S["elim"][S["elim_ptr"][f]:S["elim_ptr"][f + 1]]] = f
+    for f in range(nf):
+        anc, p = set(), fp[f]
+        while p >= 0:
+            anc.add(int(p))
+            p = fp[p]
+        for d in S["bnd"][S["bnd_ptr"][f]:S["bnd_ptr"][f + 1]]:
+            assert int(owner[d]) in anc, (f, d)
+    # at least one height has several groups in the larger case (the concurrency is exercised)
+    if case["nc"] == (16, 16):
+        assert any(lev_h.count(h) > 1 for h in set(lev_h))
