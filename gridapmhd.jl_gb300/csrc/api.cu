@@ -37,7 +37,7 @@ static void free_ctx(gbmhd_ctx* c) {
   solver_destroy(c);
   void* ptrs[] = {c->d_cellX, c->d_gidx, c->d_row, c->d_sign, c->d_xfull, c->d_fcell, c->d_fcellid,
                   c->d_flface, c->d_fprm, c->d_tab64, c->d_tab32, c->d_ftab, c->d_rowptr, c->d_col,
-                  c->d_class, c->d_offtab, c->d_val64, c->d_val32, c->d_r, c->d_xtmp, c->d_posttab};
+                  c->d_class, c->d_offtab, c->d_val64, c->d_val32, c->d_r, c->d_xtmp, c->d_posttab, c->d_val64s};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);

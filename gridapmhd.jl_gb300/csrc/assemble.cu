@@ -78,6 +78,7 @@ struct KArgs {
   void* val;          // T*
   double* r;
   DevParams prm;
+  int jpart;          // Jacobian terms: 0 all, 1 the state-independent ones, 2 convection only
 };
 
 __device__ __forceinline__ void red_add(float* p, float v) { atomicAdd(p, v); }
@@ -337,6 +338,10 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
     // part M_cd = ∫ w N_a N_b ∂_d u_c are symmetric in (a, b), so each unordered pair a ≤ b
     // (378 of them) forms them once and writes both (a, b) and (b, a); only the Picard part
     // ∫ N_a (u·∇N_b) and the AL term are formed per ordered pair.
+    // jpart 1 keeps the state-independent terms (viscous, AL, and every block but u-u below),
+    // jpart 2 the convection terms only (Picard ∫ N_a (u·∇N_b) and Newton ∫ N_a N_b ∂_d u_c)
+    const bool part_static = A.jpart != 2, part_conv = A.jpart != 1;
+    const bool cconv = conv && part_conv, cnewton = newton && part_conv;
     for (int idx = tid; idx < 27 * 28 / 2; idx += nth) {
       int a = 0, r = idx;
       while (r >= 27 - a) { r -= 27 - a; ++a; }
@@ -347,12 +352,13 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
       for (int k = 0; k < 9; ++k) Mg[k] = 0;
       for (int q = 0; q < NQ; ++q) {
         const T wd = w.wdT[q];
-        K += wd * (w.G[q][0][a] * w.G[q][0][b] + w.G[q][1][a] * w.G[q][1][b] + w.G[q][2][a] * w.G[q][2][b]);
-        if (conv) {
+        if (part_static)
+          K += wd * (w.G[q][0][a] * w.G[q][0][b] + w.G[q][1][a] * w.G[q][1][b] + w.G[q][2][a] * w.G[q][2][b]);
+        if (cconv) {
           Cab += tb.n2[q][a] * w.ugb[q][b];
           Cba += tb.n2[q][b] * w.ugb[q][a];
         }
-        if (newton) {
+        if (cnewton) {
           const T m = w.wn2[q][a] * tb.n2[q][b];
 #pragma unroll
           for (int k = 0; k < 9; ++k) Mg[k] += m * w.gu[q][k];
@@ -367,9 +373,10 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
           for (int d = 0; d < 3; ++d) {
             const int cb = OU + d * 27 + tb_;
             if (w.row[cb] < 0) continue;
+            if (!part_static && !cnewton && c != d) continue;  // nothing to add
             T v = (c == d) ? diag : (T)0;
             v += alpha * Mg[d * 3 + c];
-            if (al_u) {
+            if (al_u && part_static) {
               T s2 = 0;
               for (int k = 0; k < 4; ++k) s2 += w.Bd[k][c * 27 + ta] * w.Tm[k][d * 27 + tb_];
               v += zu * s2;
@@ -379,6 +386,7 @@ __global__ void __launch_bounds__(CELL_THREADS, CELL_MINB) k_cells(KArgs A, cons
         }
       }
     }
+    if (!part_static) continue;  // the blocks below hold no convection term
     // u-p and p-u
     for (int idx = tid; idx < 81 * 4; idx += nth) {
       const int ca = idx / 4, k = idx % 4, c = ca / 27, a = ca % 27;
@@ -926,6 +934,39 @@ int gb_upload_tables(gbmhd_ctx* ctx) {
   return 0;
 }
 
+// The state-independent terms of the FP64 Jacobian (every term but convection: viscous, AL,
+// pressure, Lorentz, Ohm, and the thin-wall facets) into ctx->d_val64s, once per parameter
+// set.  The Jacobian is affine in the state apart from convection, so a Jacobian at any state
+// is this copy plus the convection terms there: the per-step assembly does the u–u
+// convection pairs only.  Returns -1 (whole assembly instead) when the copy does not fit.
+static int static_jacobian(gbmhd_ctx* ctx, KArgs a, FArgs fa, const FacetTables* ft) {
+  if (ctx->val64s_off) return -1;
+  if (!ctx->d_val64s) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess ||
+        free_b < sizeof(double) * (size_t)ctx->nnz + ((size_t)4 << 30) ||
+        cudaMalloc(&ctx->d_val64s, sizeof(double) * std::max<int64_t>(ctx->nnz, 1)) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->d_val64s = nullptr;
+      ctx->val64s_off = true;
+      return -1;
+    }
+  }
+  if (ctx->val64s_gen == ctx->params_gen) return 0;
+  GB_CUDA(cudaMemsetAsync(ctx->d_val64s, 0, sizeof(double) * ctx->nnz, ctx->stream));
+  a.val = ctx->d_val64s;
+  a.r = nullptr;
+  a.jpart = 1;
+  fa.val = ctx->d_val64s;
+  fa.r = nullptr;
+  int rc = launch_cells<double, true, false>(ctx, a, ctx->d_tab64);
+  if (rc) return rc;
+  { if (ctx->nfacets) k_facets<double, true, false><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
+  GB_CUDA(cudaGetLastError());
+  ctx->val64s_gen = ctx->params_gen;
+  return 0;
+}
+
 // Residual (FP64) into d_r (if non-null) and Jacobian (precision) into the CSR values.
 int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_jac, int precision) {
   if (ctx->ndofs > 0)
@@ -975,7 +1016,23 @@ int gb_assemble_device(gbmhd_ctx* ctx, const double* d_x, double* d_r, int want_
         { if (d_r) k_facets<double, false, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
         { k_facets<float, true, false><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
       }
+    } else if ((rc = static_jacobian(ctx, a, fa, ft)) == 0) {
+      // FP64: the cached state-independent terms, then the convection terms at this state
+      GB_CUDA(cudaMemcpyAsync(ctx->d_val64, ctx->d_val64s, sizeof(double) * ctx->nnz, cudaMemcpyDeviceToDevice,
+                              ctx->stream));
+      a.val = ctx->d_val64;
+      fa.val = ctx->d_val64;
+      if (ctx->prm.convection != 0) {
+        a.jpart = 2;
+        if ((rc = launch_cells<double, true, false>(ctx, a, ctx->d_tab64))) return rc;
+        a.jpart = 0;
+      }
+      if (d_r) {
+        if ((rc = launch_residual(ctx, a))) return rc;
+        { if (ctx->nfacets) k_facets<double, false, true><<<(unsigned)ctx->nfacets, 64, 0, ctx->stream>>>(fa, ft); gbmhd::count_launch(); }
+      }
     } else {
+      if (rc != -1) return rc;  // a launch of the state-independent pass failed
       GB_CUDA(cudaMemsetAsync(ctx->d_val64, 0, sizeof(double) * ctx->nnz, ctx->stream));
       a.val = ctx->d_val64;
       fa.val = ctx->d_val64;

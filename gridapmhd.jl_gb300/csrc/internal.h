@@ -133,6 +133,11 @@ struct gbmhd_ctx {
   int32_t nclass = 0;
   double* d_val64 = nullptr;
   float* d_val32 = nullptr;
+  // the state-independent terms of the FP64 Jacobian (all but convection), assembled once per
+  // parameter set; an FP64 Jacobian is then this copy plus the convection terms at the state
+  double* d_val64s = nullptr;
+  int64_t val64s_gen = -1;             // params_gen of d_val64s (-1: not assembled)
+  bool val64s_off = false;             // no room for it: FP64 Jacobians assembled whole
   int jac_precision = -1;              // precision of the last assembled Jacobian
   double* d_r = nullptr;               // [ndofs] residual work vector
   double* d_xtmp = nullptr;            // [ndofs]
