@@ -472,7 +472,6 @@ static int ensure_workspace(gbmhd_ctx* ctx, int m) {
 // u, j, φ, p): ε = 1: ~29; 1e-2: 25–28; 1e-3: 15–17; 1e-4: 15–16; 1e-5: a singular pivot block.
 constexpr double kEps32 = 1e-3;
 
-// Preconditioner set-up: (u,j) factorization + mass blocks.
 // Removes the constant-pressure component from a preconditioned FGMRES direction z (z_p −= mean
 // z_p) when the all-ones vector on the p dofs is a null vector of the Jacobian (velocity fixed
 // on every wall; then also of its transpose).  The pressure is then defined up to a constant
@@ -509,6 +508,7 @@ static int project_pressure_gauge(gbmhd_ctx* ctx, double* z) {
   return 0;
 }
 
+// Preconditioner set-up: (u,j) factorization + mass blocks.
 static int setup_pc(gbmhd_ctx* ctx, int precision, int kind, double* t_setup) {
   auto t0 = std::chrono::steady_clock::now();
   Solver* s = ctx->solver;
